@@ -1,0 +1,385 @@
+"""Benchmark of the GPU-driven cull path (one JSON line on rank 0).
+
+Workload (the stress configuration): 4,000,000 render objects in [-5000,5000]^3 over 64 meshes x 4
+LODs; one step is one occlusion frame of the reference's D3D12 path (dx12Draw.cpp:590-641):
+  pass 1  blz_cull_first   — objects visible last frame (random 50% bitmask), frustum + LOD
+  pyramid blz_pyramid_build — single-pass Hi-Z over a 1920x1080 fp32 reverse-Z depth buffer
+  pass 2  blz_cull_late    — every object, frustum + Hi-Z + LOD, visibility rewritten
+Inputs are resident in HBM when the timed region starts; before each step the visibility buffer is
+restored to the 50% mask and L2 is flushed (a 512 MiB read), both outside the timed events.
+
+value  = objects per second of the device-timed frames (sum of per-step CUDA-event times).
+e2e    = the same frame through the C ABI with host buffers: per step the depth buffer (8.3 MB) and
+         the 1,000 dynamic transforms are copied from pinned host memory and both draw counts are
+         read back, all inside the timed region.
+--impl reference runs the CPU oracle (a port of the reference's shaders, all host threads) on the
+same frames.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+W, H = 1920, 1080
+DYNAMIC = 1000
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--objects", type=int, default=4_000_000)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--shape", default="", help="launch shape THREADSxOBJECTS_PER_THREAD (default: library default)")
+    ap.add_argument("--no-clock-hold", action="store_true",
+                    help="do not extend the load to 1.5 s for the clock sampler (profiling runs)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows: list[list[str]] = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) >= 9:
+                for k, name in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+# ----------------------------------------------------------------------------- reference arm
+
+def run_reference(args, rank, world):
+    """The CPU oracle on the full stress frame, every host thread; rank 0 only."""
+    if rank != 0:
+        return
+    from blitzen_gb300 import abi
+    from blitzen_gb300 import scenes as S
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    sc = S.stress_scene(args.objects, seed=args.seed)
+    v = abi.view_setup(S.fov_radians(), float(W), float(H), S.ZNEAR, 1e4, (0, 0, 0), 0, 0, W / 2, H / 2)
+    depth = O.depth_raster(v, sc.boxes, W, H)
+
+    def frame():
+        vis = sc.visibility.copy()
+        O.cull(1, v, sc, vis=vis, threads=threads)
+        p = O.pyramid_build(depth)
+        O.cull(2, v, sc, vis=vis, pyramid=p, threads=threads)
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        frame()
+    steps = max(1, args.steps)
+    times = []
+    t_end = time.perf_counter() + 60.0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        frame()
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() > t_end:
+            break
+    per = sum(times) / len(times)
+    value = args.objects / per
+    line = {
+        "impl": "reference", "metric": "objects culled/s (4M-object two-pass occlusion frame)", "value": value,
+        "unit": "objects/s", "n_gpus": world, "steps": len(times), "warmup": args.warmup,
+        "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)", "config": workload_config(args),
+        "cpu_baseline": {"value": value, "unit": "objects/s", "cores": threads, "kind": "port",
+                         "sample": f"full 4M-object frame x {len(times)} (pass 1 + pyramid + pass 2)"},
+        "e2e": {"value": value, "unit": "objects/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    return {"workload": "stress scene two-pass occlusion frame", "objects": args.objects, "meshes": 64, "lods": 256,
+            "depth": f"{W}x{H} fp32 reverse-Z, 2000 occluder boxes", "pass1_visible_fraction": 0.5,
+            "hiz": "d3d12", "record_stride": 24, "l2": "flushed between steps (512 MiB read)",
+            "parallelism": "one frame per GPU (weak scaling, no collective)"}
+
+
+# ----------------------------------------------------------------------------- our arm
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    from blitzen_gb300 import abi
+    from blitzen_gb300 import scenes as S
+    from blitzen_gb300.culler import Culler, DevicePyramid, Target
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    sc = S.stress_scene(args.objects, seed=args.seed + rank)
+    N = sc.count
+    c = Culler(local)
+    if args.shape:
+        t_, o_ = (int(x) for x in args.shape.lower().split("x"))
+        c.set_launch_shape(t_, o_)
+    c.setup_for_rendering(sc)
+    v = abi.view_setup(S.fov_radians(), float(W), float(H), S.ZNEAR, 1e4, (0, 0, 0), 0, 0, W / 2, H / 2)
+    depth = torch.zeros(W * H, dtype=torch.float32, device=dev)
+    c.raster_boxes(v, torch.from_numpy(sc.boxes.reshape(-1)).to(dev), depth, W, H)
+    vis0 = torch.from_numpy(sc.visibility.view(np.int32).copy()).to(dev)
+    vis = vis0.clone()
+    t1, t2 = Target.alloc(N, abi.STRIDE_VULKAN, dev), Target.alloc(N, abi.STRIDE_VULKAN, dev)
+    pyr = DevicePyramid(W, H, abi.HIZ_D3D12, dev)
+    # L2 flush by reading 512 MiB (a read leaves clean lines, so the next kernel pays no write-back)
+    flush = torch.ones(128 << 20, dtype=torch.int32, device=dev)
+
+    def flush_l2():
+        flush.sum(dtype=torch.int64)
+
+    stream = torch.cuda.current_stream()
+    n_prev = int(sc.visibility.sum())
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+
+    def step(e=None):
+        if e:
+            e[0].record()
+        c.draw_cull_first_pass(v, vis, t1)
+        if e:
+            e[1].record()
+        c.generate_depth_pyramid(pyr, depth)
+        if e:
+            e[2].record()
+        c.draw_cull_occlusion_pass(v, vis, pyr, t2)
+        if e:
+            e[3].record()
+
+    for _ in range(max(args.warmup, 3)):
+        vis.copy_(vis0)
+        step()
+    torch.cuda.synchronize()
+    c.check()
+    V1, _ = t1.read()
+    V2, _ = t2.read()
+
+    launches0 = c.launches
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            vis.copy_(vis0)
+            flush_l2()
+            step(ev[k])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+        launches = c.launches - launches0
+        # keep the same load on the GPU until the sampler has seen at least 1.5 s of it
+        while not args.no_clock_hold and time.perf_counter() - wall0 < 1.5:
+            for _ in range(20):
+                vis.copy_(vis0)
+                flush_l2()
+                step()
+            torch.cuda.synchronize()
+    c.check()
+    ms = [(e[0].elapsed_time(e[3])) for e in ev]
+    ms_first = [e[0].elapsed_time(e[1]) for e in ev]
+    ms_pyr = [e[1].elapsed_time(e[2]) for e in ev]
+    ms_late = [e[2].elapsed_time(e[3]) for e in ev]
+    t_step = sum(ms) / len(ms)
+    if world > 1:
+        tt = torch.tensor([t_step], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+        dist.barrier()
+    value = N * world / (t_step * 1e-3)
+
+    # roofline of the dominant kernel (pass 2) and the others, algorithmic bytes
+    stride = abi.STRIDE_VULKAN
+    mip_bytes = pyr.storage.numel() * 4
+    bytes_late = N * (8 + 32) + 4 * N + 4 * N + V2 * stride + 4
+    bytes_first = 4 * N + n_prev * (8 + 32) + V1 * stride + 4
+    bytes_pyr = W * H * 4 + mip_bytes
+    peak, peak_kind = peaks()
+    t_late = sum(ms_late) / len(ms_late)
+    t_first = sum(ms_first) / len(ms_first)
+    t_pyr = sum(ms_pyr) / len(ms_pyr)
+    ach = bytes_late / (t_late * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "cull_objects_kernel<LATE> (pass 2)", "achieved": ach, "peak": peak,
+                "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes": bytes_late, "ms": t_late,
+                "others": {
+                    "pass1": {"ms": t_first, "bytes": bytes_first, "GB/s": bytes_first / (t_first * 1e-3) / 1e9},
+                    "pyramid": {"ms": t_pyr, "bytes": bytes_pyr, "GB/s": bytes_pyr / (t_pyr * 1e-3) / 1e9},
+                    "frame": {"ms": t_step, "bytes": bytes_first + bytes_pyr + bytes_late,
+                              "GB/s": (bytes_first + bytes_pyr + bytes_late) / (t_step * 1e-3) / 1e9}}}
+    traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_file):
+        try:
+            with open(traffic_file) as f:
+                tr = json.load(f)
+            roofline["traffic"] = tr.get("cull_late_bytes_per_launch")
+        except Exception:
+            pass
+
+    # ---------------- e2e through the C ABI with host buffers
+    hdepth = torch.empty(W * H, dtype=torch.float32, pin_memory=True)
+    hdepth.copy_(depth.cpu())
+    rng = np.random.default_rng(args.seed + 99)
+    dyn_ids = np.arange(DYNAMIC, dtype=np.uint32)
+    dyn_tr = sc.transforms[:DYNAMIC].copy()
+    hcounts = torch.empty(2, dtype=torch.int32, pin_memory=True)
+    e2e_ms = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for k in range(args.warmup + args.steps):
+        vis.copy_(vis0)
+        flush_l2()
+        dyn_tr["orientation"] = S.random_unit_quaternions(rng, DYNAMIC)
+        torch.cuda.synchronize()
+        e0.record()
+        c.update_object_transform(dyn_ids, dyn_tr)
+        depth.copy_(hdepth, non_blocking=True)
+        step()
+        hcounts[0:1].copy_(t1.count, non_blocking=True)
+        hcounts[1:2].copy_(t2.count, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        if k >= args.warmup:
+            e2e_ms.append(e0.elapsed_time(e1))
+    t_e2e = sum(e2e_ms) / len(e2e_ms)
+    if world > 1:
+        tt = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e = {"value": N * world / (t_e2e * 1e-3), "unit": "objects/s", "ms_per_step": t_e2e,
+           "h2d_bytes_per_step": W * H * 4 + DYNAMIC * (32 + 4), "d2h_bytes_per_step": 8}
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        try:
+            from blitzen_gb300 import benchmarks
+            extras = benchmarks.run_extras(c, sc, dev)
+        except Exception as ex:  # extras never hide the headline line
+            extras = {"error": repr(ex)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(sc, v, depth.cpu().numpy().reshape(H, W), args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": "objects culled/s (4M-object two-pass occlusion frame)", "value": value, "unit": "objects/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": workload_config(args), "roofline": roofline,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks.summary(),
+            "wall_s_timed": wall, "draws": {"pass1": V1, "pass2": V2}, "launch_shape": c.launch_shape(),
+            "extras": extras,
+        }
+        print(json.dumps(line), flush=True)
+    c.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(sc, v, depth, seconds):
+    """The oracle (multithreaded C port of the shaders) on a bounded sample of the same frame."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    n = min(sc.count, 1_000_000)
+    from blitzen_gb300.scenes import Scene
+    sub = Scene(sc.objects[:n], sc.transforms, sc.surfaces, sc.lods, visibility=sc.visibility[:n].copy())
+    p = O.pyramid_build(depth)
+    done, t0 = 0, time.perf_counter()
+    frames = 0
+    while time.perf_counter() - t0 < seconds or frames == 0:
+        vis = sub.visibility.copy()
+        O.cull(1, v, sub, vis=vis, threads=threads)
+        p = O.pyramid_build(depth)
+        O.cull(2, v, sub, vis=vis, pyramid=p, threads=threads)
+        done += n
+        frames += 1
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "objects/s", "cores": threads, "kind": "port",
+            "sample": f"{frames} frames of the first {n} objects (pass 1 + pyramid + pass 2), {dt:.1f} s"}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,214 @@
+"""Secondary measurements reported next to the headline frame.
+
+batched_views  64 views over the resident stress scene, each with its own camera (random position in
+               the scene, random yaw and pitch), its own log-uniform object subset (1k..2M) and its own
+               pyramid from a 1920x1080 depth of occluders in front of it; frustum + Hi-Z + LOD per
+               view (the temporal pass). One persistent graph-replayed launch versus one launch per
+               view, after the autotuner picked the launch shape. Every batched result is compared
+               with the per-view result (bit-exact) before anything is timed.
+serving        the request loop over the resident scene: Poisson arrivals at 2,000 requests/s, each a
+               camera over a window of 1k..1M objects with the 1,000 dynamic objects rotated by
+               0.01 rad about random axes; p50/p99 latency from arrival to result and objects/s.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import sys
+import threading
+import time
+
+import numpy as np
+import torch
+
+from . import abi
+from . import scenes as S
+from .abi import BatchView, RenderList
+from .culler import DevicePyramid, Target, to_device
+
+W, H = 1920, 1080
+
+
+def _camera_to_world(view: abi.CameraViewData, p: np.ndarray, position) -> np.ndarray:
+    """World coordinates of camera-frame points: the view rotation transposed, plus the position."""
+    m = np.frombuffer(bytes(view.viewMatrix), np.float32).reshape(4, 4)  # m[c, r] = element (r, c)
+    # the view rotation is R^T with element (r, c) = m[c, r], so R[i][j] = m[i, j]; p_world = R p + position
+    rot = m[:3, :3].astype(np.float64)
+    return (p.astype(np.float64) @ rot.T + np.asarray(position, np.float64)).astype(np.float32)
+
+
+def build_views(culler, scene, device, n_views=64, seed=0, lo=1000, hi=2_000_000):
+    specs = S.multiview_specs(scene.count, n_views, seed=seed, lo=lo, hi=hi)
+    rng = np.random.default_rng(seed + 7)
+    views = (BatchView * n_views)()
+    keep = []
+    total = 0
+    for i, sp in enumerate(specs):
+        v = abi.view_setup(S.fov_radians(), float(W), float(H), S.ZNEAR, 1e4, sp.position, sp.yaw, sp.pitch,
+                           W / 2, H / 2)
+        objs = to_device(S.subset_objects(scene, sp.subset), device)
+        boxes_cam = S.make_occluders(rng, 2000)
+        lo_w = _camera_to_world(v, boxes_cam[:, :3], sp.position)
+        hi_w = _camera_to_world(v, boxes_cam[:, 3:], sp.position)
+        boxes = np.concatenate([np.minimum(lo_w, hi_w), np.maximum(lo_w, hi_w)], axis=1).astype(np.float32)
+        depth = torch.zeros(W * H, dtype=torch.float32, device=device)
+        culler.raster_boxes(v, torch.from_numpy(boxes.reshape(-1)).to(device), depth, W, H)
+        pyr = DevicePyramid(W, H, abi.HIZ_D3D12, device)
+        culler.generate_depth_pyramid(pyr, depth)
+        t = Target.alloc(len(sp.subset), abi.STRIDE_VULKAN, device)
+        views[i].view = v
+        views[i].list = RenderList(objs.data_ptr(), len(sp.subset))
+        views[i].mode = abi.MODE_TEMPORAL
+        views[i].pyramid = C.pointer(pyr.desc)
+        views[i].target = t.ctype()
+        keep.append((objs, pyr, t))
+        total += len(sp.subset)
+    torch.cuda.synchronize(device)
+    return views, keep, total
+
+
+def _time(fn, reps, stream):
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = []
+    for _ in range(reps):
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        out.append(a.elapsed_time(b))
+    return float(np.median(out))
+
+
+def batched_views(culler, scene, device, n_views=64, reps=20) -> dict:
+    lib = abi.load()
+    views, keep, total = build_views(culler, scene, device, n_views)
+    stream = torch.cuda.current_stream(device)
+    sp = C.c_void_p(stream.cuda_stream)
+
+    # autotuned launch shape for this batch
+    best, us = abi.LaunchShape(), C.c_float(0)
+    abi.check(lib.blz_autotune_batch(culler.ctx, views, n_views, 3, sp, C.byref(best), C.byref(us)), "autotune")
+
+    # parity: batched == per-view, record by record, before timing anything
+    abi.check(lib.blz_cull_batch(culler.ctx, views, n_views, sp), "batch")
+    batched = [k[2].read() for k in keep]
+    abi.check(lib.blz_cull_batch_per_view(culler.ctx, views, n_views, sp), "per view")
+    per_view = [k[2].read() for k in keep]
+    culler.check(stream)
+    identical = all(a[0] == b[0] and np.array_equal(a[1], b[1]) for a, b in zip(batched, per_view))
+
+    g = C.c_void_p()
+    abi.check(lib.blz_batch_graph_create(culler.ctx, views, n_views, sp, C.byref(g)), "graph")
+    try:
+        for _ in range(3):
+            lib.blz_batch_graph_launch(g, sp)
+            lib.blz_cull_batch_per_view(culler.ctx, views, n_views, sp)
+        t_graph = _time(lambda: lib.blz_batch_graph_launch(g, sp), reps, stream)
+        t_batch = _time(lambda: lib.blz_cull_batch(culler.ctx, views, n_views, sp), reps, stream)
+        t_per = _time(lambda: lib.blz_cull_batch_per_view(culler.ctx, views, n_views, sp), reps, stream)
+    finally:
+        lib.blz_batch_graph_destroy(g)
+    culler.check(stream)
+    return {
+        "views": n_views, "objects": total, "identical_to_per_view": identical,
+        "launch_shape": {"threads": best.threadsPerBlock, "objects_per_thread": best.objectsPerThread,
+                         "blocks_per_sm": best.blocksPerSm},
+        "batched_graph_ms": t_graph, "batched_ms": t_batch, "per_view_ms": t_per,
+        "batched_objects_per_s": total / (t_graph * 1e-3), "per_view_objects_per_s": total / (t_per * 1e-3),
+        "speedup": t_per / t_graph,
+        "draws": int(sum(b[0] for b in batched)),
+    }
+
+
+def serving(culler, scene, device, seconds=3.0, rate=2000.0, seed=0) -> dict:
+    lib = abi.load()
+    cfg = abi.ServeConfig(2 << 30, 4, 64, 1000, abi.STRIDE_VULKAN)
+    server = C.c_void_p()
+    abi.check(lib.blz_serve_create(culler.ctx, C.byref(cfg), C.byref(server)), "serve create")
+    rng = np.random.default_rng(seed)
+    n_req = int(seconds * rate)
+    gaps = rng.exponential(1.0 / rate, n_req)
+    arrivals = np.cumsum(gaps)
+    counts = np.exp(rng.uniform(math.log(1000), math.log(1_000_000), n_req)).astype(np.int64)
+    starts = np.array([rng.integers(0, scene.count - c) for c in counts])
+    axes = rng.normal(size=(64, 1000, 3))
+    axes = (axes / np.linalg.norm(axes, axis=2, keepdims=True)).astype(np.float32)
+    objs_dev = culler.scene_tensors[0]
+    views = []
+    for k in range(64):
+        pos = tuple(float(x) for x in rng.uniform(-4000, 4000, 3).astype(np.float32))
+        views.append(abi.view_setup(S.fov_radians(), float(W), float(H), S.ZNEAR, 1e4, pos,
+                                    float(rng.uniform(-3, 3)), float(rng.uniform(-0.5, 0.5)), W / 2, H / 2))
+    tickets = []
+    lock = threading.Lock()
+    done = threading.Event()
+    released = []
+
+    def consumer():
+        i = 0
+        while True:
+            with lock:
+                ready = i < len(tickets)
+                t = tickets[i] if ready else None
+            if not ready:
+                if done.is_set():
+                    with lock:
+                        if i >= len(tickets):
+                            return
+                    continue
+                time.sleep(20e-6)
+                continue
+            res = abi.ServeResult()
+            lib.blz_serve_wait(server, t, 60_000, C.byref(res))
+            lib.blz_serve_release(server, t)
+            released.append(res.status)
+            i += 1
+
+    th = threading.Thread(target=consumer, daemon=True)
+    old_switch = sys.getswitchinterval()
+    sys.setswitchinterval(2e-5)  # the consumer thread must get the GIL between arrivals
+    th.start()
+    t0 = time.perf_counter()
+    req = abi.ServeRequest()
+    for k in range(n_req):
+        while True:  # sleep through the gap (releasing the GIL), spin only its last 100 us
+            left = arrivals[k] - (time.perf_counter() - t0)
+            if left <= 0:
+                break
+            if left > 150e-6:
+                time.sleep(left - 100e-6)
+        req.view = views[k % 64]
+        req.list = RenderList(objs_dev.data_ptr() + int(starts[k]) * 8, int(counts[k]))
+        req.mode = abi.MODE_FRUSTUM
+        req.rotateCount = 1000
+        req.rotateAxes = axes[k % 64].ctypes.data
+        req.rotateAngle = 0.01
+        req.copyToHost = 0
+        t = C.c_uint64()
+        abi.check(lib.blz_serve_submit(server, C.byref(req), C.byref(t)), "submit")
+        with lock:
+            tickets.append(t.value)
+    done.set()
+    th.join()
+    sys.setswitchinterval(old_switch)
+    elapsed = time.perf_counter() - t0
+    st = abi.ServeStats()
+    lib.blz_serve_stats(server, C.byref(st))
+    lib.blz_serve_destroy(server)
+    return {"requests": n_req, "offered_rate_per_s": rate, "elapsed_s": elapsed, "p50_ms": st.p50Ms,
+            "p99_ms": st.p99Ms, "mean_ms": st.meanMs, "max_ms": st.maxMs, "batches": st.batches,
+            "max_batch": st.maxBatchSize, "max_concurrent_batches": st.maxConcurrentBatches,
+            "objects_per_s": float(counts.sum()) / elapsed, "errors": int(sum(1 for s in released if s))}
+
+
+def run_extras(culler, scene, device) -> dict:
+    out = {}
+    try:
+        out["batched_views"] = batched_views(culler, scene, device)
+    except Exception as ex:
+        out["batched_views"] = {"error": repr(ex)}
+    try:
+        out["serving"] = serving(culler, scene, device)
+    except Exception as ex:
+        out["serving"] = {"error": repr(ex)}
+    return out

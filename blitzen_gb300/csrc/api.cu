@@ -1,0 +1,553 @@
+// api.cu — the C ABI of libblz_cull.so: context, scene residency, pyramid, culls, batches.
+//
+// Host-side counterpart of the reference's cull dispatch code: the renderer members and static
+// dispatch helpers of src/Renderer/BlitzenVulkan/vulkanDraw.cpp:107-622 and
+// src/Renderer/BlitzenDX12/dx12Draw.cpp:114-415, without the graphics API around them.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "api_internal.h"
+
+namespace blz {
+
+thread_local std::string g_lastError;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_lastError = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(BLZ_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+static void release_scene(blz_ctx* c) {
+    for (void* p : c->ownedScene) cudaFree(p);
+    c->ownedScene.clear();
+    c->scene = SceneT{};
+    c->defaultObjects = nullptr;
+    c->defaultCount = 0;
+    c->hasScene = false;
+}
+
+SceneT scene_tables(const blz_ctx* c) { return c->scene; }
+
+PyramidT pyramid_view(const BlzPyramid* p) {
+    PyramidT v{};
+    if (!p) return v;
+    v.data = p->data;
+    v.width = p->width;
+    v.height = p->height;
+    v.mipCount = p->mipCount;
+    v.mode = p->mode;
+    for (uint32_t i = 0; i < BLZ_PYRAMID_MAX_MIPS; ++i) v.mipOffset[i] = p->mipOffset[i];
+    return v;
+}
+
+int check_pyramid(const BlzPyramid* p, bool required) {
+    if (!p) return required ? fail(BLZ_ERR_INVALID_ARGUMENT, "a pyramid is required for this pass") : BLZ_OK;
+    if (!p->data) return fail(BLZ_ERR_INVALID_ARGUMENT, "pyramid has no storage");
+    if (p->mipCount == 0 || p->mipCount > BLZ_PYRAMID_MAX_MIPS) return fail(BLZ_ERR_INVALID_ARGUMENT, "pyramid mipCount %u out of range", p->mipCount);
+    if (p->mode > BLZ_HIZ_VULKAN) return fail(BLZ_ERR_INVALID_ARGUMENT, "unknown pyramid mode %u", p->mode);
+    if (p->width == 0 || p->height == 0) return fail(BLZ_ERR_INVALID_ARGUMENT, "pyramid extent is zero");
+    return BLZ_OK;
+}
+
+int check_target(const BlzCullTarget* t) {
+    if (!t) return fail(BLZ_ERR_INVALID_ARGUMENT, "target is NULL");
+    if (t->stride != BLZ_STRIDE_VULKAN && t->stride != BLZ_STRIDE_D3D12)
+        return fail(BLZ_ERR_INVALID_ARGUMENT, "record stride must be 24 or 32, got %u", t->stride);
+    if (!t->drawCount) return fail(BLZ_ERR_INVALID_ARGUMENT, "target drawCount is NULL");
+    if (t->capacity > 0 && !t->commands) return fail(BLZ_ERR_INVALID_ARGUMENT, "target commands is NULL");
+    if (reinterpret_cast<uintptr_t>(t->commands) % 16 != 0)
+        return fail(BLZ_ERR_INVALID_ARGUMENT, "target commands must be 16-byte aligned");
+    return BLZ_OK;
+}
+
+int resolve_list(const blz_ctx* c, BlzRenderList list, const BlzRenderObject** objs, uint32_t* count) {
+    if (!c->hasScene) return fail(BLZ_ERR_NO_SCENE, "no scene uploaded");
+    if (list.objects) {
+        *objs = list.objects;
+        *count = list.count;
+    } else {
+        *objs = c->defaultObjects;
+        *count = list.count ? list.count : c->defaultCount;
+        if (*count > c->defaultCount) return fail(BLZ_ERR_INVALID_ARGUMENT, "render list count %u exceeds the scene's %u", *count, c->defaultCount);
+    }
+    if (*count > 0 && !*objs) return fail(BLZ_ERR_INVALID_ARGUMENT, "render list has no objects");
+    if (reinterpret_cast<uintptr_t>(*objs) % 8 != 0) return fail(BLZ_ERR_INVALID_ARGUMENT, "render list must be 8-byte aligned");
+    if (*count >= (1u << 30)) return fail(BLZ_ERR_INVALID_ARGUMENT, "render list count %u exceeds 2^30", *count);
+    return BLZ_OK;
+}
+
+int ensure_chunk_scratch(blz_ctx* c, size_t chunks, size_t chunkSize) {
+    const size_t objects = chunks * chunkSize;
+    if (objects <= c->chunkObjects && chunks <= c->chunkSlots) return BLZ_OK;
+    size_t wantObj = objects > c->chunkObjects ? objects + objects / 4 : c->chunkObjects;
+    size_t wantSlots = chunks > c->chunkSlots ? chunks + chunks / 4 + 64 : c->chunkSlots;
+    if (c->chunkMem) {
+        cudaDeviceSynchronize();
+        cudaFree(c->chunkMem);
+        c->chunkMem = nullptr;
+        c->chunkObjects = c->chunkSlots = 0;
+    }
+    const size_t bytes = wantObj * sizeof(uint2) + 2 * wantSlots * sizeof(uint32_t) + 256;
+    if (cudaMalloc(&c->chunkMem, bytes) != cudaSuccess) return fail(BLZ_ERR_OUT_OF_MEMORY, "object-cull scratch of %zu bytes", bytes);
+    c->chunkObjects = wantObj;
+    c->chunkSlots = wantSlots;
+    return BLZ_OK;
+}
+
+void bind_chunk_scratch(blz_ctx* c, PipeParams& p) {
+    char* m = static_cast<char*>(c->chunkMem);
+    p.staged = reinterpret_cast<uint2*>(m);
+    p.chunkCount = reinterpret_cast<uint32_t*>(m + c->chunkObjects * sizeof(uint2));
+    p.chunkPrefix = p.chunkCount + c->chunkSlots;
+    p.doneBlocks = c->pyrCounter + 1;
+    p.scratch = c->scratch;
+}
+
+int ensure_states(blz_ctx* c, size_t states) {
+    if (states <= c->stateCapacity) return BLZ_OK;
+    return fail(BLZ_ERR_CAPACITY, "%zu tile states needed, the context holds %zu", states, c->stateCapacity);
+}
+
+}  // namespace blz
+
+using namespace blz;
+
+extern "C" {
+
+const char* blz_last_error(void) { return g_lastError.c_str(); }
+
+const char* blz_version(void) { return "blz_cull 0.1 (sm_103a)"; }
+
+int blz_ctx_create(int device, blz_ctx** out) {
+    if (!out) return fail(BLZ_ERR_INVALID_ARGUMENT, "outCtx is NULL");
+    *out = nullptr;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    blz_ctx* c = new blz_ctx();
+    c->device = device;
+    cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device);
+    c->stateCapacity = kDefaultStateCapacity;
+    const size_t bytes = kScratchHeaderBytes + c->stateCapacity * sizeof(unsigned long long);
+    e = cudaMalloc(&c->scratchMem, bytes);
+    if (e != cudaSuccess) { delete c; return e == cudaErrorMemoryAllocation ? fail(BLZ_ERR_OUT_OF_MEMORY, "scratch allocation failed") : cuda_fail(e, "cudaMalloc scratch"); }
+    e = cudaMemset(c->scratchMem, 0, bytes);
+    if (e == cudaSuccess) {
+        // epoch starts at 1 so zeroed tile states never read as published
+        const unsigned int one = 1u;
+        e = cudaMemcpy(static_cast<char*>(c->scratchMem) + 4, &one, sizeof one, cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&c->pyrCounter, sizeof(unsigned int) * 4);
+    if (e == cudaSuccess) e = cudaMemset(c->pyrCounter, 0, sizeof(unsigned int) * 4);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->pinned, kPinnedBytes);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->pinnedDone, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        int rc = cuda_fail(e, "context setup");
+        blz_ctx_destroy(c);
+        return rc;
+    }
+    c->scratch = static_cast<Scratch*>(c->scratchMem);
+    *out = c;
+    return BLZ_OK;
+}
+
+int blz_ctx_destroy(blz_ctx* c) {
+    if (!c) return BLZ_OK;
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    release_scene(c);
+    if (c->scratchMem) cudaFree(c->scratchMem);
+    if (c->pyrCounter) cudaFree(c->pyrCounter);
+    if (c->pinned) cudaFreeHost(c->pinned);
+    if (c->pinnedDone) cudaEventDestroy(c->pinnedDone);
+    if (c->batchDev) cudaFree(c->batchDev);
+    if (c->stagingDev) cudaFree(c->stagingDev);
+    if (c->chunkMem) cudaFree(c->chunkMem);
+    delete c;
+    return BLZ_OK;
+}
+
+uint64_t blz_ctx_launch_count(const blz_ctx* c) { return c ? c->launches.load() : 0; }
+
+int blz_ctx_check(blz_ctx* c, blz_stream_t stream, uint32_t* flagsOut) {
+    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    cudaError_t e = cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    unsigned int hdr[5];
+    e = cudaMemcpy(hdr, c->scratchMem, sizeof hdr, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "status read");
+    const uint32_t flags = hdr[4];
+    if (flags) {
+        unsigned int zero = 0u;
+        cudaMemcpy(static_cast<char*>(c->scratchMem) + 16, &zero, sizeof zero, cudaMemcpyHostToDevice);
+    }
+    if (flags & BLZ_FLAG_TIMEOUT) {
+        // a timed-out launch may have left the ticket mid-way: restart the protocol on a new epoch
+        unsigned int fresh[3] = {0u, hdr[1] + 2u, 0u};
+        cudaMemcpy(c->scratchMem, fresh, sizeof fresh, cudaMemcpyHostToDevice);
+        cudaMemset(c->pyrCounter, 0, sizeof(unsigned int));
+    }
+    if (flagsOut) *flagsOut = flags;
+    if (flags & BLZ_FLAG_TIMEOUT) return fail(BLZ_ERR_TIMEOUT, "a device-side wait timed out (flags 0x%x)", flags);
+    if (flags & BLZ_FLAG_BAD_INDEX) return fail(BLZ_ERR_BAD_INDEX, "a scene id was out of range (flags 0x%x)", flags);
+    if (flags & (BLZ_FLAG_COMMAND_OVERFLOW | BLZ_FLAG_INSTANCE_OVERFLOW))
+        return fail(BLZ_ERR_CAPACITY, "an output buffer overflowed (flags 0x%x)", flags);
+    return BLZ_OK;
+}
+
+// ------------------------------------------------------------------ scene
+
+int blz_scene_upload(blz_ctx* c, const BlzSceneDesc* s, uint32_t flags, blz_stream_t stream) {
+    if (!c || !s) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or scene is NULL");
+    if (flags > BLZ_SCENE_BORROW_DEVICE) return fail(BLZ_ERR_INVALID_ARGUMENT, "unknown scene flags 0x%x", flags);
+    if ((s->transformCount && !s->transforms) || (s->surfaceCount && !s->surfaces) || (s->lodCount && !s->lods) ||
+        (s->clusterCount && !s->clusters) || (s->renderObjectCount && !s->renderObjects))
+        return fail(BLZ_ERR_INVALID_ARGUMENT, "a scene table has a count but no pointer");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    cudaSetDevice(c->device);
+    release_scene(c);
+    SceneT t{};
+    t.transformCount = s->transformCount;
+    t.surfaceCount = s->surfaceCount;
+    t.lodCount = s->lodCount;
+    t.clusterCount = s->clusterCount;
+    if (flags == BLZ_SCENE_BORROW_DEVICE) {
+        t.objects = s->renderObjects;
+        t.transforms = s->transforms;
+        t.surfaces = s->surfaces;
+        t.lods = s->lods;
+        t.clusters = s->clusters;
+    } else {
+        auto up = [&](const void* src, size_t bytes, const void** dst) -> cudaError_t {
+            *dst = nullptr;
+            if (!bytes) return cudaSuccess;
+            void* d = nullptr;
+            cudaError_t e = cudaMalloc(&d, bytes);
+            if (e != cudaSuccess) return e;
+            c->ownedScene.push_back(d);
+            *dst = d;
+            return cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, st);
+        };
+        cudaError_t e = up(s->renderObjects, sizeof(BlzRenderObject) * (size_t)s->renderObjectCount, reinterpret_cast<const void**>(&t.objects));
+        if (e == cudaSuccess) e = up(s->transforms, sizeof(BlzMeshTransform) * (size_t)s->transformCount, reinterpret_cast<const void**>(&t.transforms));
+        if (e == cudaSuccess) e = up(s->surfaces, sizeof(BlzPrimitiveSurface) * (size_t)s->surfaceCount, reinterpret_cast<const void**>(&t.surfaces));
+        if (e == cudaSuccess) e = up(s->lods, sizeof(BlzLodData) * (size_t)s->lodCount, reinterpret_cast<const void**>(&t.lods));
+        if (e == cudaSuccess) e = up(s->clusters, sizeof(BlzCluster) * (size_t)s->clusterCount, reinterpret_cast<const void**>(&t.clusters));
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            release_scene(c);
+            return e == cudaErrorMemoryAllocation ? fail(BLZ_ERR_OUT_OF_MEMORY, "scene allocation failed") : cuda_fail(e, "scene upload");
+        }
+    }
+    if (reinterpret_cast<uintptr_t>(t.transforms) % 16 || reinterpret_cast<uintptr_t>(t.surfaces) % 16 ||
+        reinterpret_cast<uintptr_t>(t.lods) % 16 || reinterpret_cast<uintptr_t>(t.clusters) % 16 ||
+        reinterpret_cast<uintptr_t>(t.objects) % 8) {
+        release_scene(c);
+        return fail(BLZ_ERR_INVALID_ARGUMENT, "scene tables must be 16-byte aligned (render objects 8-byte)");
+    }
+    c->scene = t;
+    c->defaultObjects = t.objects;
+    c->defaultCount = s->renderObjectCount;
+    c->hasScene = true;
+    return BLZ_OK;
+}
+
+int blz_scene_device_tables(const blz_ctx* c, BlzSceneDesc* out) {
+    if (!c || !out) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or out is NULL");
+    if (!c->hasScene) return fail(BLZ_ERR_NO_SCENE, "no scene uploaded");
+    out->renderObjects = c->defaultObjects;
+    out->renderObjectCount = c->defaultCount;
+    out->transforms = c->scene.transforms;
+    out->transformCount = c->scene.transformCount;
+    out->surfaces = c->scene.surfaces;
+    out->surfaceCount = c->scene.surfaceCount;
+    out->lods = c->scene.lods;
+    out->lodCount = c->scene.lodCount;
+    out->clusters = c->scene.clusters;
+    out->clusterCount = c->scene.clusterCount;
+    return BLZ_OK;
+}
+
+int blz_transforms_update_device(blz_ctx* c, const uint32_t* ids, const BlzMeshTransform* in, uint32_t n, blz_stream_t stream) {
+    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (!c->hasScene) return fail(BLZ_ERR_NO_SCENE, "no scene uploaded");
+    if (n && (!ids || !in)) return fail(BLZ_ERR_INVALID_ARGUMENT, "ids or transforms is NULL");
+    cudaError_t e = launch_transforms_scatter(const_cast<BlzMeshTransform*>(c->scene.transforms), c->scene.transformCount, ids, in, n,
+                                              &c->scratch->status, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "transforms scatter launch");
+    if (n) c->launches++;
+    return BLZ_OK;
+}
+
+int blz_transforms_update(blz_ctx* c, const uint32_t* ids, const BlzMeshTransform* in, uint32_t n, blz_stream_t stream) {
+    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (!c->hasScene) return fail(BLZ_ERR_NO_SCENE, "no scene uploaded");
+    if (n == 0) return BLZ_OK;
+    if (!ids || !in) return fail(BLZ_ERR_INVALID_ARGUMENT, "ids or transforms is NULL");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const size_t need = (size_t)n * (sizeof(uint32_t) + sizeof(BlzMeshTransform)) + 64;
+    if (need > kPinnedBytes) return fail(BLZ_ERR_CAPACITY, "%u transforms exceed the staging buffer", n);
+    int rc = ensure_staging(c, need);
+    if (rc != BLZ_OK) return rc;
+    cudaEventSynchronize(c->pinnedDone);  // the previous staged copy has left the pinned buffer
+    char* h = static_cast<char*>(c->pinned);
+    const size_t tOff = 0, iOff = ((size_t)n * sizeof(BlzMeshTransform) + 63) & ~size_t(63);
+    memcpy(h + tOff, in, (size_t)n * sizeof(BlzMeshTransform));
+    memcpy(h + iOff, ids, (size_t)n * sizeof(uint32_t));
+    char* d = static_cast<char*>(c->stagingDev);
+    cudaError_t e = cudaMemcpyAsync(d, h, iOff + (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaEventRecord(c->pinnedDone, st);
+    if (e != cudaSuccess) return cuda_fail(e, "transform staging copy");
+    return blz_transforms_update_device(c, reinterpret_cast<const uint32_t*>(d + iOff), reinterpret_cast<const BlzMeshTransform*>(d + tOff), n, stream);
+}
+
+int blz_transforms_rotate(blz_ctx* c, const uint32_t* ids, const float* axes, float angle, uint32_t n, BlzMeshTransform* dst,
+                          blz_stream_t stream) {
+    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (!c->hasScene) return fail(BLZ_ERR_NO_SCENE, "no scene uploaded");
+    if (n && (!ids || !axes)) return fail(BLZ_ERR_INVALID_ARGUMENT, "ids or axes is NULL");
+    BlzMeshTransform* out = dst;
+    if (!out) {
+        // in place: rotate into staging, then scatter back (a kernel may not read and write the same rows)
+        return fail(BLZ_ERR_INVALID_ARGUMENT, "in-place rotation needs a destination buffer; pass dDst and scatter it");
+    }
+    cudaError_t e = launch_transforms_rotate(c->scene.transforms, c->scene.transformCount, ids, axes, angle, n, out, &c->scratch->status,
+                                             reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "transforms rotate launch");
+    if (n) c->launches++;
+    return BLZ_OK;
+}
+
+// ------------------------------------------------------------------ pyramid
+
+static uint32_t mip_levels(uint32_t w, uint32_t h) {  // blitML.h:95-107
+    uint32_t n = 0;
+    while (w > 1 || h > 1) {
+        ++n;
+        w /= 2;
+        h /= 2;
+    }
+    return n;
+}
+
+static uint32_t previous_pow2(uint32_t v) {  // blitML.h:54-62
+    uint32_t r = 1;
+    while (r * 2 < v) r *= 2;
+    return r;
+}
+
+uint64_t blz_pyramid_layout(uint32_t dw, uint32_t dh, uint32_t mode, BlzPyramid* out) {
+    if (!out || dw == 0 || dh == 0 || mode > BLZ_HIZ_VULKAN) return 0;
+    memset(out, 0, sizeof *out);
+    out->mode = mode;
+    out->depthWidth = dw;
+    out->depthHeight = dh;
+    if (mode == BLZ_HIZ_D3D12) {
+        out->width = (dw >> 1) ? (dw >> 1) : 1u;
+        out->height = (dh >> 1) ? (dh >> 1) : 1u;
+    } else {
+        out->width = previous_pow2(dw);
+        out->height = previous_pow2(dh);
+    }
+    uint32_t n = mip_levels(out->width, out->height);
+    if (n == 0) n = 1;
+    if (n > BLZ_PYRAMID_MAX_MIPS) return 0;
+    out->mipCount = n;
+    uint64_t at = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t w = out->width >> i, h = out->height >> i;
+        w = w ? w : 1u;
+        h = h ? h : 1u;
+        out->mipOffset[i] = static_cast<uint32_t>(at);
+        at += (uint64_t)w * h;
+    }
+    return at * sizeof(float);
+}
+
+int blz_pyramid_build(blz_ctx* c, const BlzPyramid* p, const float* depth, blz_stream_t stream) {
+    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    int rc = check_pyramid(p, true);
+    if (rc != BLZ_OK) return rc;
+    if (!depth) return fail(BLZ_ERR_INVALID_ARGUMENT, "depth is NULL");
+    if (p->depthWidth == 0 || p->depthHeight == 0) return fail(BLZ_ERR_INVALID_ARGUMENT, "pyramid has no depth extent");
+    PyramidBuildParams bp{};
+    bp.depth = depth;
+    bp.depthWidth = p->depthWidth;
+    bp.depthHeight = p->depthHeight;
+    bp.data = p->data;
+    bp.width = p->width;
+    bp.height = p->height;
+    bp.mipCount = p->mipCount;
+    bp.mode = p->mode;
+    for (uint32_t i = 0; i < BLZ_PYRAMID_MAX_MIPS; ++i) bp.mipOffset[i] = p->mipOffset[i];
+    bp.counter = c->pyrCounter;
+    uint32_t launches = 0;
+    cudaError_t e = launch_pyramid_build(bp, reinterpret_cast<cudaStream_t>(stream), &launches);
+    if (e != cudaSuccess) return cuda_fail(e, "pyramid launch");
+    c->launches += launches;
+    return BLZ_OK;
+}
+
+int blz_depth_raster_boxes(blz_ctx* c, const BlzCameraViewData* view, const float* boxes, uint32_t boxCount, float* depth,
+                           uint32_t width, uint32_t height, blz_stream_t stream) {
+    if (!c || !view || !depth) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx, view or depth is NULL");
+    if (boxCount && !boxes) return fail(BLZ_ERR_INVALID_ARGUMENT, "boxes is NULL");
+    if (width == 0 || height == 0 || (uint64_t)width * height >= (1ull << 31)) return fail(BLZ_ERR_INVALID_ARGUMENT, "bad depth extent");
+    uint32_t launches = 0;
+    cudaError_t e = launch_depth_raster(*view, boxes, boxCount, depth, width, height, reinterpret_cast<cudaStream_t>(stream), &launches);
+    if (e != cudaSuccess) return cuda_fail(e, "depth raster launch");
+    c->launches += launches;
+    return BLZ_OK;
+}
+
+// ------------------------------------------------------------------ single-view culls
+
+static int object_cull(blz_ctx* c, uint32_t mode, const BlzCameraViewData* view, BlzRenderList list, uint32_t* vis,
+                       const BlzPyramid* pyr, const BlzCullTarget* target, blz_stream_t stream) {
+    if (!c || !view) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or view is NULL");
+    int rc = check_target(target);
+    if (rc != BLZ_OK) return rc;
+    const BlzRenderObject* objs = nullptr;
+    uint32_t count = 0;
+    rc = resolve_list(c, list, &objs, &count);
+    if (rc != BLZ_OK) return rc;
+    if ((mode == BLZ_MODE_FIRST || mode == BLZ_MODE_LATE) && count && !vis) return fail(BLZ_ERR_INVALID_ARGUMENT, "visibility buffer is NULL");
+    if (mode == BLZ_MODE_LATE || mode == BLZ_MODE_TEMPORAL) {
+        rc = check_pyramid(pyr, true);
+        if (rc != BLZ_OK) return rc;
+    }
+    const uint32_t tile = c->single_tile();
+    uint32_t tiles = (count + tile - 1) / tile;
+    if (tiles == 0) tiles = 1;  // an empty list still gets one chunk, and its draw count is written
+    rc = ensure_chunk_scratch(c, tiles, tile);
+    if (rc != BLZ_OK) return rc;
+    PipeParams p{};
+    p.sc = c->scene;
+    p.single.view = *view;
+    p.single.objects = objs;
+    p.single.count = count;
+    p.single.mode = mode;
+    p.single.vis = vis;
+    p.single.pyr = pyramid_view(pyr);
+    p.single.cmds = static_cast<uint8_t*>(target->commands);
+    p.single.stride = target->stride;
+    p.single.capacity = target->capacity;
+    p.single.drawCount = target->drawCount;
+    p.single.dynT = nullptr;
+    p.single.dynCount = 0;
+    p.views = nullptr;
+    p.tileStart = nullptr;
+    p.viewCount = 1;
+    p.totalTiles = tiles;
+    bind_chunk_scratch(c, p);
+    cudaError_t e = launch_object_cull(mode, p, c->singleThreads, c->singleOpt, c->smCount, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "cull launch");
+    c->launches += 2;  // decide + scatter
+    return BLZ_OK;
+}
+
+int blz_cull_frustum(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, const BlzCullTarget* target, blz_stream_t s) {
+    return object_cull(c, BLZ_MODE_FRUSTUM, view, list, nullptr, nullptr, target, s);
+}
+
+int blz_cull_first(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, const uint32_t* vis, const BlzCullTarget* target,
+                   blz_stream_t s) {
+    return object_cull(c, BLZ_MODE_FIRST, view, list, const_cast<uint32_t*>(vis), nullptr, target, s);
+}
+
+int blz_cull_late(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, uint32_t* vis, const BlzPyramid* pyr,
+                  const BlzCullTarget* target, blz_stream_t s) {
+    return object_cull(c, BLZ_MODE_LATE, view, list, vis, pyr, target, s);
+}
+
+int blz_cull_temporal(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, const BlzPyramid* pyr,
+                      const BlzCullTarget* target, blz_stream_t s) {
+    return object_cull(c, BLZ_MODE_TEMPORAL, view, list, nullptr, pyr, target, s);
+}
+
+int blz_cull_instanced(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, BlzLodInstanceCounter* counters,
+                       uint32_t* instances, uint32_t instanceCapacity, uint32_t slotsPerLod, const BlzCullTarget* target,
+                       blz_stream_t s) {
+    if (!c || !view) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or view is NULL");
+    int rc = check_target(target);
+    if (rc != BLZ_OK) return rc;
+    const BlzRenderObject* objs = nullptr;
+    uint32_t count = 0;
+    rc = resolve_list(c, list, &objs, &count);
+    if (rc != BLZ_OK) return rc;
+    if (!counters) return fail(BLZ_ERR_INVALID_ARGUMENT, "counters is NULL");
+    if (instanceCapacity && !instances) return fail(BLZ_ERR_INVALID_ARGUMENT, "instances is NULL");
+    const uint32_t nL = c->scene.lodCount;
+    if (nL == 0) return fail(BLZ_ERR_INVALID_ARGUMENT, "the scene has no LODs");
+    if (nL > kMaxInstancedLods) return fail(BLZ_ERR_INVALID_ARGUMENT, "instanced cull supports up to %u LODs, scene has %u", kMaxInstancedLods, nL);
+    const uint32_t tiles = (count + instanced_tile_size() - 1) / instanced_tile_size();
+    rc = ensure_states(c, (size_t)(tiles ? tiles : 1) * nL);
+    if (rc != BLZ_OK) return rc;
+    InstancedParams p{};
+    p.sc = c->scene;
+    p.objects = objs;
+    p.count = count;
+    p.stride = target->stride;
+    p.counters = counters;
+    p.instances = instances;
+    p.instanceCapacity = instanceCapacity;
+    p.slotsPerLod = slotsPerLod;
+    p.cmds = static_cast<uint8_t*>(target->commands);
+    p.capacity = target->capacity;
+    p.drawCount = target->drawCount;
+    p.scratch = c->scratch;
+    cudaError_t e = launch_instanced_cull(p, *view, reinterpret_cast<cudaStream_t>(s));
+    if (e != cudaSuccess) return cuda_fail(e, "instanced cull launch");
+    c->launches++;
+    return BLZ_OK;
+}
+
+int blz_cull_clusters(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, const BlzPyramid* pyr,
+                      const BlzCullTarget* target, uint32_t* clusterIds, blz_stream_t s) {
+    if (!c || !view) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or view is NULL");
+    int rc = check_target(target);
+    if (rc != BLZ_OK) return rc;
+    const BlzRenderObject* objs = nullptr;
+    uint32_t count = 0;
+    rc = resolve_list(c, list, &objs, &count);
+    if (rc != BLZ_OK) return rc;
+    rc = check_pyramid(pyr, false);
+    if (rc != BLZ_OK) return rc;
+    if (!c->scene.clusters && c->scene.clusterCount) return fail(BLZ_ERR_INVALID_ARGUMENT, "scene has no cluster table");
+    const uint32_t tiles = (count + cluster_tile_objects() - 1) / cluster_tile_objects();
+    rc = ensure_states(c, tiles);
+    if (rc != BLZ_OK) return rc;
+    ClusterParams p{};
+    p.sc = c->scene;
+    p.objects = objs;
+    p.count = count;
+    p.stride = target->stride;
+    p.pyr = pyramid_view(pyr);
+    p.hasPyramid = pyr ? 1u : 0u;
+    p.capacity = target->capacity;
+    p.cmds = static_cast<uint8_t*>(target->commands);
+    p.clusterIds = clusterIds;
+    p.drawCount = target->drawCount;
+    p.scratch = c->scratch;
+    cudaError_t e = launch_cluster_cull(p, *view, reinterpret_cast<cudaStream_t>(s));
+    if (e != cudaSuccess) return cuda_fail(e, "cluster cull launch");
+    c->launches++;
+    return BLZ_OK;
+}
+
+// ------------------------------------------------------------------ view constants
+
+}  // extern "C"

@@ -1,0 +1,80 @@
+// api_internal.h — context layout and helpers shared by the C ABI translation units.
+#pragma once
+
+#include <atomic>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace blz {
+
+constexpr size_t kDefaultStateCapacity = size_t(1) << 22;  // 4M tile states (32 MiB)
+constexpr size_t kPinnedBytes = size_t(8) << 20;            // transform / batch staging
+constexpr uint32_t kMaxInstancedLods = 4096;                // shared-memory bucket histograms
+
+}  // namespace blz
+
+struct blz_ctx {
+    int device = 0;
+    int smCount = 0;
+    void* scratchMem = nullptr;        // Scratch header + tile states
+    blz::Scratch* scratch = nullptr;
+    size_t stateCapacity = 0;
+    unsigned int* pyrCounter = nullptr;
+    void* pinned = nullptr;            // pinned host staging
+    cudaEvent_t pinnedDone = nullptr;  // last copy out of `pinned` has completed
+    void* stagingDev = nullptr;        // device side of the staging
+    size_t stagingBytes = 0;
+    void* batchDev = nullptr;          // device BatchViewDev[] + tileStart[]
+    size_t batchBytes = 0;
+    void* chunkMem = nullptr;          // object-cull staging: records, chunk counts, chunk prefixes
+    size_t chunkObjects = 0;           // staged-record capacity
+    size_t chunkSlots = 0;             // chunk count capacity
+    bool hasScene = false;
+    blz::SceneT scene{};
+    const BlzRenderObject* defaultObjects = nullptr;
+    uint32_t defaultCount = 0;
+    std::vector<void*> ownedScene;
+    std::atomic<uint64_t> launches{0};
+    BlzLaunchShape shape{256, 2, 0, 0};   // batch launches
+    uint32_t singleThreads = 256, singleOpt = 2;  // single-view launches
+
+    uint32_t single_tile() const { return singleThreads * singleOpt; }
+};
+
+namespace blz {
+
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+PyramidT pyramid_view(const BlzPyramid* p);
+int check_pyramid(const BlzPyramid* p, bool required);
+int check_target(const BlzCullTarget* t);
+int resolve_list(const blz_ctx* c, BlzRenderList list, const BlzRenderObject** objs, uint32_t* count);
+int ensure_states(blz_ctx* c, size_t states);
+
+// Object-cull scratch for `chunks` chunks of `chunkSize` objects (grown on demand; a call that
+// grows it synchronises the device first).
+int ensure_chunk_scratch(blz_ctx* c, size_t chunks, size_t chunkSize);
+void bind_chunk_scratch(blz_ctx* c, PipeParams& p);
+
+inline int ensure_staging(blz_ctx* c, size_t bytes) {
+    if (bytes <= c->stagingBytes) return 0;
+    if (c->stagingDev) {
+        cudaStreamSynchronize(nullptr);
+        cudaDeviceSynchronize();
+        cudaFree(c->stagingDev);
+        c->stagingDev = nullptr;
+        c->stagingBytes = 0;
+    }
+    size_t want = bytes < kPinnedBytes ? kPinnedBytes : bytes;
+    cudaError_t e = cudaMalloc(&c->stagingDev, want);
+    if (e != cudaSuccess) return fail(BLZ_ERR_OUT_OF_MEMORY, "staging allocation of %zu bytes failed", want);
+    c->stagingBytes = want;
+    return 0;
+}
+
+}  // namespace blz

@@ -1,0 +1,151 @@
+// kernels.h — launch parameters and launchers shared by the kernel files and the C ABI layer.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/blz_cull.h"
+#include "../../include/blz_types.h"
+
+namespace blz {
+
+struct Scratch;
+
+#ifndef __CUDACC__
+// Host-only translation units see the device structs as opaque layouts of the same size.
+struct Vec3 { float x, y, z; };
+#endif
+
+struct SceneTablesHost {
+    const BlzRenderObject* objects;
+    const BlzMeshTransform* transforms;
+    const BlzPrimitiveSurface* surfaces;
+    const BlzLodData* lods;
+    const BlzCluster* clusters;
+    uint32_t transformCount, surfaceCount, lodCount, clusterCount;
+};
+
+struct PyramidViewHost {
+    const float* data;
+    uint32_t width, height, mipCount, mode;
+    uint32_t mipOffset[BLZ_PYRAMID_MAX_MIPS];
+};
+
+}  // namespace blz
+
+#ifdef __CUDACC__
+#include "blz_device.cuh"
+#endif
+
+namespace blz {
+
+#ifdef __CUDACC__
+using SceneT = SceneTables;
+using PyramidT = PyramidView;
+static_assert(sizeof(SceneTables) == sizeof(SceneTablesHost), "scene table layout");
+static_assert(sizeof(PyramidView) == sizeof(PyramidViewHost), "pyramid layout");
+#else
+using SceneT = SceneTablesHost;
+using PyramidT = PyramidViewHost;
+#endif
+
+constexpr int kObjThreads = 256;
+constexpr int kObjOpt = 2;
+constexpr uint32_t kMaxTiles = 1u << 20;             // tile states held by one scratch
+constexpr size_t kScratchHeaderBytes = 128;          // Scratch fields before the state array
+
+// Device copy of one view of a cull launch (its uniform, render list, mode, buffers).
+struct BatchViewDev {
+    BlzCameraViewData view;
+    const BlzRenderObject* objects;
+    uint32_t count;
+    uint32_t mode;
+    uint32_t* vis;
+    PyramidT pyr;
+    uint8_t* cmds;
+    uint32_t stride;
+    uint32_t capacity;
+    uint32_t* drawCount;
+    const BlzMeshTransform* dynT;
+    uint32_t dynCount;
+    uint32_t pad;
+};
+
+// Parameters of the object-cull kernels: one view inline (single-view launches) or an array of
+// views in device memory with the first chunk of each (viewCount + 1 entries), plus the scratch
+// the decide kernel stages compacted records in (chunk c owns staged[c * chunkSize ...]).
+struct PipeParams {
+    SceneT sc;
+    BatchViewDev single;
+    const BatchViewDev* views;
+    const uint32_t* tileStart;
+    uint32_t viewCount;
+    uint32_t totalTiles;   // chunks over all views
+    Scratch* scratch;      // status word
+    uint2* staged;         // [totalTiles * chunkSize] (objectId, lodId)
+    uint32_t* chunkCount;  // [totalTiles]
+    uint32_t* chunkPrefix; // [totalTiles]
+    unsigned int* doneBlocks;
+};
+
+struct InstancedParams {
+    SceneT sc;
+    const BlzRenderObject* objects;
+    uint32_t count;
+    uint32_t stride;
+    BlzLodInstanceCounter* counters;
+    uint32_t* instances;
+    uint32_t instanceCapacity;
+    uint32_t slotsPerLod;
+    uint8_t* cmds;
+    uint32_t capacity;
+    uint32_t pad;
+    uint32_t* drawCount;
+    uint32_t* lodBlockCounts;   // scratch: [tiles][lodCount] per-tile LOD histograms
+    Scratch* scratch;
+};
+
+struct ClusterParams {
+    SceneT sc;
+    const BlzRenderObject* objects;
+    uint32_t count;
+    uint32_t stride;
+    PyramidT pyr;
+    uint32_t hasPyramid;
+    uint32_t capacity;
+    uint8_t* cmds;
+    uint32_t* clusterIds;
+    uint32_t* drawCount;
+    Scratch* scratch;
+};
+
+struct PyramidBuildParams {
+    const float* depth;
+    uint32_t depthWidth, depthHeight;
+    float* data;
+    uint32_t width, height, mipCount, mode;
+    uint32_t mipOffset[BLZ_PYRAMID_MAX_MIPS];
+    unsigned int* counter;   // scratch: blocks finished
+};
+
+uint32_t object_tile_size();
+bool single_shape_supported(uint32_t threads, uint32_t opt);
+cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t threads, uint32_t opt, int smCount,
+                               cudaStream_t s);
+bool batch_shape_supported(uint32_t threads, uint32_t opt);
+cudaError_t launch_batch_cull(const PipeParams& p, uint32_t threads, uint32_t opt, uint32_t blocksPerSm, int smCount,
+                              cudaStream_t s);
+uint32_t instanced_tile_size();
+cudaError_t launch_instanced_cull(const InstancedParams& p, const BlzCameraViewData& view, cudaStream_t s);
+uint32_t cluster_tile_objects();
+cudaError_t launch_cluster_cull(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s);
+cudaError_t launch_pyramid_build(const PyramidBuildParams& p, cudaStream_t s, uint32_t* launches);
+cudaError_t launch_transforms_scatter(BlzMeshTransform* table, uint32_t tableCount, const uint32_t* ids,
+                                      const BlzMeshTransform* in, uint32_t n, unsigned int* status, cudaStream_t s);
+cudaError_t launch_transforms_rotate(const BlzMeshTransform* table, uint32_t tableCount, const uint32_t* ids,
+                                     const float* axes, float angle, uint32_t n, BlzMeshTransform* dst,
+                                     unsigned int* status, cudaStream_t s);
+cudaError_t launch_depth_raster(const BlzCameraViewData& view, const float* boxes, uint32_t boxCount, float* depth,
+                                uint32_t width, uint32_t height, cudaStream_t s, uint32_t* launches);
+
+}  // namespace blz

@@ -1,0 +1,171 @@
+// pyramid.cu — single-pass Hi-Z depth pyramid.
+//
+// The reference builds the pyramid with one dispatch per mip and a barrier between them
+// (src/Renderer/BlitzenDX12/dx12Draw.cpp:248-277, src/Renderer/BlitzenVulkan/vulkanDraw.cpp:579-614).
+// Here one launch builds every mip: each block owns a 64x64 tile of mip 0, writes it, and reduces
+// it through mips 1..6 in shared memory (a 64-texel tile reaches 1 texel at mip 6); the last block
+// to finish (device counter) builds the few remaining small mips from mip 6 in global memory.
+//
+// Texel rules:
+//   D3D12   depthPyramid.cs.hlsl:16-26 — min(r, min(g, min(b, a))) of the 2x2 Loads at
+//           (2x, 2y) .. (2x+1, 2y+1) of the previous level (the depth buffer for mip 0); a Load
+//           outside the previous level returns 0.
+//   VULKAN  DepthPyramidGeneration.comp.glsl:15-19 — MIN-reduction bilinear footprint of the
+//           previous level at ((x + 0.5) / w, (y + 0.5) / h), clamp to edge. Mip 0 is a power of
+//           two, so from mip 1 on the footprint of texel x is {2x, 2x+1} (or {0} on a 1-wide level)
+//           and stays inside the block's tile.
+#include "blz_device.cuh"
+#include "kernels.h"
+
+namespace blz {
+
+constexpr int kPyrThreads = 256;
+constexpr uint32_t kPyrTile = 64;
+constexpr uint32_t kPyrInTileLevels = 6;
+
+__device__ __forceinline__ float load_or_zero(const float* img, uint32_t w, uint32_t h, uint64_t x, uint64_t y) {
+    return (x < w && y < h) ? __ldcg(img + y * w + x) : 0.0f;
+}
+
+// D3D12 2x2 min over an image in global memory (depth buffer or a finished mip).
+__device__ __forceinline__ float d3d_texel(const float* src, uint32_t sw, uint32_t sh, uint32_t x, uint32_t y) {
+    const uint64_t x0 = 2ull * x, y0 = 2ull * y;
+    const float r = load_or_zero(src, sw, sh, x0, y0);
+    const float g = load_or_zero(src, sw, sh, x0 + 1, y0);
+    const float b = load_or_zero(src, sw, sh, x0, y0 + 1);
+    const float a = load_or_zero(src, sw, sh, x0 + 1, y0 + 1);
+    return fmin_nan(r, fmin_nan(g, fmin_nan(b, a)));
+}
+
+// Footprint indices of texel x of a w-wide level sampling an sw-wide source (Vulkan sampler).
+__device__ __forceinline__ void vk_footprint(uint32_t x, uint32_t w, uint32_t sw, uint32_t& i0, uint32_t& i1) {
+    const float s = BLZ_FD(BLZ_FA(static_cast<float>(x), 0.5f), static_cast<float>(w));
+    const float u = BLZ_FS(BLZ_FM(s, static_cast<float>(sw)), 0.5f);
+    const float fu = floorf(u);
+    const float au = BLZ_FS(u, fu);
+    long long a = to_index(fu);
+    long long b = (au > 0.0f) ? a + 1 : a;
+    const long long hi = static_cast<long long>(sw) - 1;
+    a = a < 0 ? 0 : (a > hi ? hi : a);
+    b = b < 0 ? 0 : (b > hi ? hi : b);
+    i0 = static_cast<uint32_t>(a);
+    i1 = static_cast<uint32_t>(b);
+}
+
+template <uint32_t MODE>
+__device__ __forceinline__ float level_texel_global(const float* src, uint32_t sw, uint32_t sh, uint32_t x, uint32_t y,
+                                                    uint32_t w, uint32_t h) {
+    if (MODE == BLZ_HIZ_D3D12) return d3d_texel(src, sw, sh, x, y);
+    uint32_t i0, i1, j0, j1;
+    vk_footprint(x, w, sw, i0, i1);
+    vk_footprint(y, h, sh, j0, j1);
+    float m = __int_as_float(0x7fc00000);
+    m = fmin_nan(m, __ldcg(src + static_cast<size_t>(j0) * sw + i0));
+    m = fmin_nan(m, __ldcg(src + static_cast<size_t>(j0) * sw + i1));
+    m = fmin_nan(m, __ldcg(src + static_cast<size_t>(j1) * sw + i0));
+    m = fmin_nan(m, __ldcg(src + static_cast<size_t>(j1) * sw + i1));
+    return m;
+}
+
+template <uint32_t MODE>
+__global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuildParams p) {
+    __shared__ float sA[kPyrTile * kPyrTile];
+    __shared__ float sB[(kPyrTile / 2) * (kPyrTile / 2)];
+    __shared__ int s_last;
+    const uint32_t X0 = blockIdx.x * kPyrTile, Y0 = blockIdx.y * kPyrTile;
+    const uint32_t W0 = p.width, H0 = p.height;
+
+    // mip 0 from the depth buffer
+    for (uint32_t idx = threadIdx.x; idx < kPyrTile * kPyrTile; idx += kPyrThreads) {
+        const uint32_t lx = idx & (kPyrTile - 1), ly = idx / kPyrTile;
+        const uint32_t gx = X0 + lx, gy = Y0 + ly;
+        float v = 0.0f;
+        if (gx < W0 && gy < H0) {
+            v = level_texel_global<MODE>(p.depth, p.depthWidth, p.depthHeight, gx, gy, W0, H0);
+            p.data[p.mipOffset[0] + static_cast<size_t>(gy) * W0 + gx] = v;
+        }
+        sA[idx] = v;
+    }
+    __syncthreads();
+
+    // mips 1..6 inside the tile
+    float* src = sA;
+    float* dst = sB;
+    uint32_t S = kPyrTile;  // previous level's tile extent
+    for (uint32_t k = 1; k <= kPyrInTileLevels && k < p.mipCount; ++k) {
+        const uint32_t Sk = S >> 1;
+        const uint32_t Wp = mip_dim(W0, k - 1), Hp = mip_dim(H0, k - 1);
+        const uint32_t Wk = mip_dim(W0, k), Hk = mip_dim(H0, k);
+        const uint32_t Xp = X0 >> (k - 1), Yp = Y0 >> (k - 1);
+        const uint32_t Xk = X0 >> k, Yk = Y0 >> k;
+        for (uint32_t idx = threadIdx.x; idx < Sk * Sk; idx += kPyrThreads) {
+            const uint32_t lx = idx % Sk, ly = idx / Sk;
+            const uint32_t gx = Xk + lx, gy = Yk + ly;
+            float v = 0.0f;
+            if (gx < Wk && gy < Hk) {
+                if (MODE == BLZ_HIZ_D3D12) {
+                    const uint32_t x0 = 2u * gx, y0 = 2u * gy;
+                    const uint32_t l0 = 2u * lx, m0 = 2u * ly;
+                    const float r = (x0 < Wp && y0 < Hp) ? src[m0 * S + l0] : 0.0f;
+                    const float g = (x0 + 1 < Wp && y0 < Hp) ? src[m0 * S + l0 + 1] : 0.0f;
+                    const float b = (x0 < Wp && y0 + 1 < Hp) ? src[(m0 + 1) * S + l0] : 0.0f;
+                    const float a = (x0 + 1 < Wp && y0 + 1 < Hp) ? src[(m0 + 1) * S + l0 + 1] : 0.0f;
+                    v = fmin_nan(r, fmin_nan(g, fmin_nan(b, a)));
+                } else {
+                    uint32_t i0, i1, j0, j1;
+                    vk_footprint(gx, Wk, Wp, i0, i1);
+                    vk_footprint(gy, Hk, Hp, j0, j1);
+                    // the footprint lies in this tile (power-of-two levels); clamp defensively
+                    const uint32_t a0 = min(i0 - Xp, S - 1), a1 = min(i1 - Xp, S - 1);
+                    const uint32_t b0 = min(j0 - Yp, S - 1), b1 = min(j1 - Yp, S - 1);
+                    float m = __int_as_float(0x7fc00000);
+                    m = fmin_nan(m, src[b0 * S + a0]);
+                    m = fmin_nan(m, src[b0 * S + a1]);
+                    m = fmin_nan(m, src[b1 * S + a0]);
+                    m = fmin_nan(m, src[b1 * S + a1]);
+                    v = m;
+                }
+                p.data[p.mipOffset[k] + static_cast<size_t>(gy) * Wk + gx] = v;
+            }
+            dst[idx] = v;
+        }
+        __syncthreads();
+        float* t = src;
+        src = dst;
+        dst = t;
+        S = Sk;
+    }
+
+    if (p.mipCount <= kPyrInTileLevels + 1) return;
+
+    // the last block to finish builds the small mips that span several tiles
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(p.counter, 1u) == gridDim.x * gridDim.y - 1u) ? 1 : 0;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (uint32_t k = kPyrInTileLevels + 1; k < p.mipCount; ++k) {
+        const uint32_t Wp = mip_dim(W0, k - 1), Hp = mip_dim(H0, k - 1);
+        const uint32_t Wk = mip_dim(W0, k), Hk = mip_dim(H0, k);
+        const float* prev = p.data + p.mipOffset[k - 1];
+        float* out = p.data + p.mipOffset[k];
+        for (uint32_t idx = threadIdx.x; idx < Wk * Hk; idx += kPyrThreads) {
+            const uint32_t gx = idx % Wk, gy = idx / Wk;
+            out[idx] = level_texel_global<MODE>(prev, Wp, Hp, gx, gy, Wk, Hk);
+        }
+        __threadfence_block();
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *p.counter = 0u;
+}
+
+cudaError_t launch_pyramid_build(const PyramidBuildParams& p, cudaStream_t s, uint32_t* launches) {
+    dim3 grid((p.width + kPyrTile - 1) / kPyrTile, (p.height + kPyrTile - 1) / kPyrTile);
+    if (p.mode == BLZ_HIZ_VULKAN) pyramid_kernel<BLZ_HIZ_VULKAN><<<grid, kPyrThreads, 0, s>>>(p);
+    else pyramid_kernel<BLZ_HIZ_D3D12><<<grid, kPyrThreads, 0, s>>>(p);
+    if (launches) *launches += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace blz

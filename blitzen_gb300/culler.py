@@ -1,0 +1,230 @@
+"""Host-side mirror of the reference renderer's cull interface, over libblz_cull.so.
+
+The reference reaches its cull through renderer members (SetupForRendering, UpdateObjectTransform,
+DrawFrame; src/Renderer/BlitzenVulkan/vulkanRenderer.h:20-40, src/Renderer/BlitzenDX12/dx12Renderer.h:22-43)
+and static dispatch helpers (DrawCullFirstPass, GenerateDepthPyramid, DrawCullOcclusionPass,
+DrawInstanceCullPass, PreClusterDrawCull/ClusterCull; vulkanDraw.cpp:107-622, dx12Draw.cpp:114-415).
+`Culler` offers those operations by the same names, with device buffers held in torch tensors
+(torch is only the allocator and the stream here; every pass is a libblz_cull kernel).
+
+Errors: the reference returns 0 and logs; here every failing call raises `BlzError` with the
+library's message. There is no CPU fallback: a missing library is an error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import abi
+from .abi import BlzError, CameraViewData, CullTarget, Pyramid, RenderList, SceneDesc, check
+from .scenes import Scene
+
+
+def _stream_ptr(stream: torch.cuda.Stream | None) -> C.c_void_p:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _dev_u32(n: int, device) -> torch.Tensor:
+    return torch.zeros(max(int(n), 1), dtype=torch.int32, device=device)
+
+
+def to_device(a: np.ndarray, device) -> torch.Tensor:
+    """A numpy array's bytes in a device tensor (int32 words when the size allows, else bytes)."""
+    raw = np.ascontiguousarray(a).view(np.uint8).reshape(-1)
+    if raw.nbytes % 4 == 0:
+        return torch.from_numpy(raw.view(np.int32).copy()).to(device)
+    return torch.from_numpy(raw.copy()).to(device)
+
+
+@dataclass
+class Target:
+    """Indirect-command output (binding 7 / u0) and its draw count (binding 9 / u1)."""
+    commands: torch.Tensor
+    count: torch.Tensor
+    stride: int
+    capacity: int
+
+    @classmethod
+    def alloc(cls, capacity: int, stride: int = abi.STRIDE_VULKAN, device="cuda") -> "Target":
+        words = max(int(capacity), 1) * stride // 4
+        return cls(torch.zeros(words, dtype=torch.int32, device=device), _dev_u32(1, device), stride, int(capacity))
+
+    def ctype(self) -> CullTarget:
+        return CullTarget(self.commands.data_ptr(), self.stride, self.capacity, self.count.data_ptr())
+
+    def read(self) -> tuple[int, np.ndarray]:
+        """(drawCount, records[min(count, capacity), stride/4] as uint32)."""
+        n = int(self.count.cpu().numpy().view(np.uint32)[0])
+        m = min(n, self.capacity)
+        recs = self.commands[: m * self.stride // 4].cpu().numpy().view(np.uint32).reshape(m, self.stride // 4)
+        return n, recs
+
+
+class DevicePyramid:
+    """A Hi-Z pyramid in device memory with its descriptor (BlzPyramid)."""
+
+    def __init__(self, depth_w: int, depth_h: int, mode: int = abi.HIZ_D3D12, device="cuda"):
+        self.desc, nbytes = abi.pyramid_layout(depth_w, depth_h, mode)
+        self.storage = torch.zeros(nbytes // 4, dtype=torch.float32, device=device)
+        self.desc.data = self.storage.data_ptr()
+
+    @property
+    def extent(self) -> tuple[int, int]:
+        return self.desc.width, self.desc.height
+
+    def mip(self, level: int) -> np.ndarray:
+        h, w = self.desc.mip_shape(level)
+        off = self.desc.mipOffset[level]
+        return self.storage[off: off + w * h].cpu().numpy().reshape(h, w)
+
+
+class Culler:
+    """One library context: resident scene tables, scratch and status word for one stream."""
+
+    def __init__(self, device: int = 0):
+        if not torch.cuda.is_available():
+            raise RuntimeError("libblz_cull needs a CUDA device")
+        self.lib = abi.load()
+        self.device = torch.device("cuda", device)
+        torch.cuda.set_device(self.device)
+        h = C.c_void_p()
+        check(self.lib.blz_ctx_create(device, C.byref(h)), "blz_ctx_create")
+        self.ctx = h
+        self._keep: list[torch.Tensor] = []
+        self.scene_count = 0
+
+    def close(self) -> None:
+        if self.ctx:
+            self.lib.blz_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------ scene
+
+    def setup_for_rendering(self, scene: Scene, stream=None) -> None:
+        """Makes the scene's tables resident (SetupForRendering / StaticBuffersInit)."""
+        tens = [to_device(a, self.device) if len(a) else None for a in
+                (scene.objects, scene.transforms, scene.surfaces, scene.lods, scene.clusters)]
+        self._keep = [t for t in tens if t is not None]
+        ptr = [t.data_ptr() if t is not None else None for t in tens]
+        desc = SceneDesc(ptr[0], scene.count, ptr[1], len(scene.transforms), ptr[2], len(scene.surfaces),
+                         ptr[3], len(scene.lods), ptr[4], len(scene.clusters))
+        torch.cuda.synchronize(self.device)
+        check(self.lib.blz_scene_upload(self.ctx, C.byref(desc), abi.SCENE_BORROW_DEVICE, _stream_ptr(stream)),
+              "blz_scene_upload")
+        self.scene_count = scene.count
+        self.scene_tensors = tens
+
+    def update_object_transform(self, ids: np.ndarray, transforms: np.ndarray, stream=None) -> None:
+        """UpdateObjectTransform for many ids (host arrays, staged through pinned memory)."""
+        ids = np.ascontiguousarray(ids, np.uint32)
+        tr = np.ascontiguousarray(transforms)
+        check(self.lib.blz_transforms_update(self.ctx, ids.ctypes.data, tr.ctypes.data, len(ids), _stream_ptr(stream)),
+              "blz_transforms_update")
+
+    def rotate_transforms(self, ids: torch.Tensor, axes: torch.Tensor, angle: float, dst: torch.Tensor, stream=None):
+        check(self.lib.blz_transforms_rotate(self.ctx, ids.data_ptr(), axes.data_ptr(), angle, ids.numel(),
+                                             dst.data_ptr(), _stream_ptr(stream)), "blz_transforms_rotate")
+
+    # ------------------------------------------------------------------ passes
+
+    @staticmethod
+    def _list(objects: torch.Tensor | None, count: int | None) -> RenderList:
+        if objects is None:
+            return RenderList(None, count or 0)
+        return RenderList(objects.data_ptr(), count if count is not None else objects.numel() * 4 // 8)
+
+    def draw_cull(self, view: CameraViewData, target: Target, objects=None, count=None, stream=None) -> None:
+        """Frustum + LOD (TransparentDrawCull / drawCull.cs.hlsl)."""
+        t = target.ctype()
+        check(self.lib.blz_cull_frustum(self.ctx, C.byref(view), self._list(objects, count), C.byref(t),
+                                        _stream_ptr(stream)), "blz_cull_frustum")
+
+    def draw_cull_first_pass(self, view, visibility: torch.Tensor, target: Target, objects=None, count=None, stream=None):
+        """Occlusion pass 1 (InitialDrawCull / drawOccFirst)."""
+        t = target.ctype()
+        check(self.lib.blz_cull_first(self.ctx, C.byref(view), self._list(objects, count), visibility.data_ptr(),
+                                      C.byref(t), _stream_ptr(stream)), "blz_cull_first")
+
+    def generate_depth_pyramid(self, pyramid: DevicePyramid, depth: torch.Tensor, stream=None) -> None:
+        check(self.lib.blz_pyramid_build(self.ctx, C.byref(pyramid.desc), depth.data_ptr(), _stream_ptr(stream)),
+              "blz_pyramid_build")
+
+    def draw_cull_occlusion_pass(self, view, visibility: torch.Tensor, pyramid: DevicePyramid, target: Target,
+                                 objects=None, count=None, stream=None):
+        """Occlusion pass 2 (LateDrawCull / drawOccLate)."""
+        t = target.ctype()
+        check(self.lib.blz_cull_late(self.ctx, C.byref(view), self._list(objects, count), visibility.data_ptr(),
+                                     C.byref(pyramid.desc), C.byref(t), _stream_ptr(stream)), "blz_cull_late")
+
+    def draw_cull_temporal(self, view, pyramid: DevicePyramid, target: Target, objects=None, count=None, stream=None):
+        t = target.ctype()
+        check(self.lib.blz_cull_temporal(self.ctx, C.byref(view), self._list(objects, count), C.byref(pyramid.desc),
+                                         C.byref(t), _stream_ptr(stream)), "blz_cull_temporal")
+
+    def draw_instance_cull_pass(self, view, counters: torch.Tensor, instances: torch.Tensor, slots_per_lod: int,
+                                target: Target, objects=None, count=None, stream=None):
+        t = target.ctype()
+        check(self.lib.blz_cull_instanced(self.ctx, C.byref(view), self._list(objects, count), counters.data_ptr(),
+                                          instances.data_ptr(), instances.numel(), slots_per_lod, C.byref(t),
+                                          _stream_ptr(stream)), "blz_cull_instanced")
+
+    def cluster_cull(self, view, target: Target, pyramid: DevicePyramid | None = None,
+                     cluster_ids: torch.Tensor | None = None, objects=None, count=None, stream=None):
+        t = target.ctype()
+        check(self.lib.blz_cull_clusters(self.ctx, C.byref(view), self._list(objects, count),
+                                         C.byref(pyramid.desc) if pyramid else None, C.byref(t),
+                                         cluster_ids.data_ptr() if cluster_ids is not None else None,
+                                         _stream_ptr(stream)), "blz_cull_clusters")
+
+    def raster_boxes(self, view, boxes: torch.Tensor, depth: torch.Tensor, width: int, height: int, stream=None):
+        check(self.lib.blz_depth_raster_boxes(self.ctx, C.byref(view), boxes.data_ptr(), boxes.numel() // 6,
+                                              depth.data_ptr(), width, height, _stream_ptr(stream)),
+              "blz_depth_raster_boxes")
+
+    # ------------------------------------------------------------------ launch shape
+
+    def set_launch_shape(self, threads: int, objects_per_thread: int, blocks_per_sm: int = 0) -> None:
+        check(self.lib.blz_set_launch_shape(self.ctx, C.byref(abi.LaunchShape(threads, objects_per_thread,
+                                                                              blocks_per_sm, 0))),
+              "blz_set_launch_shape")
+
+    def launch_shape(self) -> dict:
+        s = abi.LaunchShape()
+        check(self.lib.blz_get_launch_shape(self.ctx, C.byref(s)), "blz_get_launch_shape")
+        return {"threads": s.threadsPerBlock, "objects_per_thread": s.objectsPerThread, "blocks_per_sm": s.blocksPerSm}
+
+    # ------------------------------------------------------------------ status
+
+    def check(self, stream=None) -> int:
+        """Synchronises and returns the device status flags (raises on overflow / bad index / timeout)."""
+        f = C.c_uint32(0)
+        rc = self.lib.blz_ctx_check(self.ctx, _stream_ptr(stream), C.byref(f))
+        if rc != 0:
+            raise BlzError(rc, "blz_ctx_check", self.lib.blz_last_error().decode())
+        return int(f.value)
+
+    def flags(self, stream=None) -> int:
+        """Like check(), but returns the flags instead of raising."""
+        f = C.c_uint32(0)
+        self.lib.blz_ctx_check(self.ctx, _stream_ptr(stream), C.byref(f))
+        return int(f.value)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.blz_ctx_launch_count(self.ctx))

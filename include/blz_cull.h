@@ -1,0 +1,348 @@
+/*
+ * blz_cull.h — C ABI of the GB300 culling library (libblz_cull.so).
+ *
+ * The library replaces the GPU-driven culling path of the Blitzen renderer: the cull compute
+ * shaders, the depth-pyramid shader and the host code that binds and dispatches them. Every
+ * entry point names the reference interface it stands in for (paths inside the Blitzen project).
+ *
+ * Conventions
+ *  - Every function returns an int status: BLZ_OK (0) or one of the BLZ_ERR_* codes. The
+ *    reference returns uint8_t 1/0 plus a log line; blz_last_error() gives the message of the
+ *    last failing call on the calling thread.
+ *  - Pointers documented as "device" are CUDA device pointers the caller owns; "host" pointers
+ *    are read before the call returns (or copied to pinned staging first).
+ *  - Work is enqueued on the caller's stream (a cudaStream_t passed as blz_stream_t; NULL is the
+ *    legacy default stream) and runs asynchronously, exactly like a recorded dispatch.
+ *  - Results are deterministic: records are written in ascending render-object order (clusters:
+ *    object order, then cluster order), instance lists in ascending object order, instanced
+ *    commands in ascending LOD order. The reference orders them by atomic arrival; any stable
+ *    order is a valid output of the reference, and this is the one its serial execution gives.
+ *  - Capacity overflow never writes out of bounds: records past the capacity are counted but
+ *    not stored, and a device-side status flag is raised (read it with blz_ctx_check).
+ *  - One context serves one stream at a time; two streams need two contexts (each context
+ *    owns the scratch state of its single-pass kernels).
+ */
+#ifndef BLZ_CULL_H
+#define BLZ_CULL_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "blz_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* blz_stream_t; /* identical to cudaStream_t */
+typedef struct blz_ctx blz_ctx;
+typedef struct blz_server blz_server;
+typedef struct blz_batch_graph blz_batch_graph;
+
+/* ---------------------------------------------------------------- status codes */
+enum {
+    BLZ_OK = 0,
+    BLZ_ERR_INVALID_ARGUMENT = 1,
+    BLZ_ERR_CAPACITY = 2,      /* an output buffer was too small; extra records were dropped */
+    BLZ_ERR_OUT_OF_MEMORY = 3,
+    BLZ_ERR_TIMEOUT = 4,       /* a bounded wait expired (device or host side) */
+    BLZ_ERR_CUDA = 5,          /* a CUDA runtime call failed; see blz_last_error() */
+    BLZ_ERR_BAD_INDEX = 6,     /* a scene table referenced an id past the end of its table */
+    BLZ_ERR_NOT_READY = 7,     /* asynchronous result not available yet */
+    BLZ_ERR_NO_SCENE = 8       /* cull called before blz_scene_upload */
+};
+
+/* Device-side status flags, OR-ed by kernels and read (and cleared) by blz_ctx_check. */
+enum {
+    BLZ_FLAG_COMMAND_OVERFLOW = 1u,  /* more visible records than BlzCullTarget.capacity */
+    BLZ_FLAG_INSTANCE_OVERFLOW = 2u, /* a LOD received more instances than its slot range */
+    BLZ_FLAG_BAD_INDEX = 4u,         /* transformId / surfaceId / LOD range out of range */
+    BLZ_FLAG_TIMEOUT = 8u            /* a bounded spin-wait in a single-pass kernel gave up */
+};
+
+/* Record strides: Vulkan IndirectDrawData (24 B) or D3D12 IndirectDrawCmd (32 B). */
+#define BLZ_STRIDE_VULKAN 24u
+#define BLZ_STRIDE_D3D12 32u
+
+/* Hi-Z semantics. D3D12 (default): mip 0 = depth extent / 2, 2x2 integer-load min per level,
+ * one-texel Load in the occlusion test (depthPyramid.cs.hlsl, hlslMath.hlsl:58-78).
+ * VULKAN: mip 0 = previous power of two of the depth extent, min-reduction bilinear footprint
+ * (DepthPyramidGeneration.comp.glsl, CullingShaderData.glsl:60-73). */
+#define BLZ_HIZ_D3D12 0u
+#define BLZ_HIZ_VULKAN 1u
+#define BLZ_PYRAMID_MAX_MIPS 16u
+
+/* ---------------------------------------------------------------- context */
+
+/* Creates a context on a CUDA device: scratch for the single-pass kernels, the status word and
+ * pinned staging. Replaces the renderer setup of the cull resources
+ * (src/Renderer/BlitzenVulkan/vulkanRendererSetup.cpp:453-522, vulkanRenderer.h:20-40). */
+int blz_ctx_create(int device, blz_ctx** outCtx);
+int blz_ctx_destroy(blz_ctx* ctx);
+
+/* Message of the last failing call made on this thread ("" if none). */
+const char* blz_last_error(void);
+
+/* Library version string and the number of kernels this build contains. */
+const char* blz_version(void);
+
+/* Synchronises the stream, returns the device status flags raised since the last check and
+ * clears them. Returns BLZ_ERR_CAPACITY / BLZ_ERR_BAD_INDEX / BLZ_ERR_TIMEOUT when the matching
+ * flag is set, else BLZ_OK. flagsOut may be NULL. Stands in for the reference's fence wait plus
+ * the validation it never had (vulkanData.h:196-197). */
+int blz_ctx_check(blz_ctx* ctx, blz_stream_t stream, uint32_t* flagsOut);
+
+/* Number of this library's kernel launches enqueued by the context so far. */
+uint64_t blz_ctx_launch_count(const blz_ctx* ctx);
+
+/* ---------------------------------------------------------------- scene residency */
+
+typedef struct BlzSceneDesc {
+    const BlzRenderObject* renderObjects;   /* default render list (may be NULL) */
+    uint32_t renderObjectCount;
+    const BlzMeshTransform* transforms;
+    uint32_t transformCount;
+    const BlzPrimitiveSurface* surfaces;
+    uint32_t surfaceCount;
+    const BlzLodData* lods;
+    uint32_t lodCount;
+    const BlzCluster* clusters;              /* may be NULL when no cluster culling is done */
+    uint32_t clusterCount;
+} BlzSceneDesc;
+
+#define BLZ_SCENE_COPY_FROM_HOST 0u   /* pointers are host memory; the library copies */
+#define BLZ_SCENE_BORROW_DEVICE 1u    /* pointers are device memory the caller keeps alive */
+
+/* Makes a scene resident: render objects, transforms, surfaces, LODs, clusters in the reference
+ * layouts. Replaces StaticBuffersInit / SetupForRendering
+ * (src/Renderer/BlitzenVulkan/vulkanRendererSetup.cpp:453-522, dx12Renderer.h:22-43). */
+int blz_scene_upload(blz_ctx* ctx, const BlzSceneDesc* scene, uint32_t flags, blz_stream_t stream);
+
+/* Device pointers of the resident tables (for callers that build render lists on the device). */
+int blz_scene_device_tables(const blz_ctx* ctx, BlzSceneDesc* out);
+
+/* Overwrites transforms[ids[i]] = transforms_in[i] for i < n. ids and transforms_in are host
+ * arrays (staged through pinned memory). Replaces UpdateObjectTransform + UpdateBuffers
+ * (src/Renderer/BlitzenVulkan/vulkanDraw.cpp:46-60,816-820). */
+int blz_transforms_update(blz_ctx* ctx, const uint32_t* ids, const BlzMeshTransform* transformsIn,
+                          uint32_t n, blz_stream_t stream);
+
+/* Same, with ids and transforms already in device memory. */
+int blz_transforms_update_device(blz_ctx* ctx, const uint32_t* dIds, const BlzMeshTransform* dTransforms,
+                                 uint32_t n, blz_stream_t stream);
+
+/* Device-side rotation of dynamic objects: for i < n, writes dDst[i] = transforms[dIds[i]] with its
+ * orientation replaced by q_i (x) orientation (Hamilton product), q_i = (sin(a/2) axis_i, cos(a/2)),
+ * axis_i = dAxes[3i..3i+2] (unit vectors), a = angle. dDst is a device buffer of n transforms (it
+ * can be scattered back with blz_transforms_update_device, or used as a per-view override of the
+ * dynamic rows in a batch). The dynamic-object rotation of src/Game/blitzenObject.cpp:30-46 as a
+ * kernel. */
+int blz_transforms_rotate(blz_ctx* ctx, const uint32_t* dIds, const float* dAxes, float angle,
+                          uint32_t n, BlzMeshTransform* dDst, blz_stream_t stream);
+
+/* ---------------------------------------------------------------- depth pyramid */
+
+typedef struct BlzPyramid {
+    float* data;                 /* device storage, mips back to back, each row-major */
+    uint32_t width;              /* mip 0 extent = CameraViewData.pyramidWidth */
+    uint32_t height;             /* mip 0 extent = CameraViewData.pyramidHeight */
+    uint32_t mipCount;
+    uint32_t mode;               /* BLZ_HIZ_D3D12 or BLZ_HIZ_VULKAN */
+    uint32_t depthWidth;         /* source depth-buffer extent */
+    uint32_t depthHeight;
+    uint32_t mipOffset[BLZ_PYRAMID_MAX_MIPS]; /* offset of each mip in floats */
+} BlzPyramid;
+
+/* Fills every field but data for a depth buffer of depthWidth x depthHeight and returns the
+ * bytes data must hold (0 on bad arguments). D3D12: mip 0 = max(1, W>>1) x max(1, H>>1)
+ * (src/Renderer/BlitzenDX12/dx12RNDResources.cpp:96-118); Vulkan: PreviousPow2 of each
+ * (src/Renderer/BlitzenVulkan/vulkanResources.cpp:87-95). Mip count per GetDepthPyramidMipLevels
+ * (src/BlitzenMathLibrary/blitML.h:95-107). */
+uint64_t blz_pyramid_layout(uint32_t depthWidth, uint32_t depthHeight, uint32_t mode, BlzPyramid* out);
+
+/* Builds every mip from a device fp32 reverse-Z depth buffer (row-major, depthWidth floats per
+ * row) in one single-pass launch. Replaces GenerateDepthPyramid
+ * (src/Renderer/BlitzenDX12/dx12Draw.cpp:224-288, src/Renderer/BlitzenVulkan/vulkanDraw.cpp:554-622)
+ * and its per-mip dispatches of depthPyramid.cs.hlsl / DepthPyramidGeneration.comp.glsl. */
+int blz_pyramid_build(blz_ctx* ctx, const BlzPyramid* pyramid, const float* dDepth, blz_stream_t stream);
+
+/* Rasterises axis-aligned occluder boxes (world space, 6 floats each: min xyz, max xyz) into a
+ * device fp32 reverse-Z depth buffer for one view: clears to 0, then every box writes
+ * zNear / zFarthestCorner over its projected screen rectangle (max-depth test). A stand-in for
+ * the reference's depth pre-pass, which is a graphics-API rasterisation. */
+int blz_depth_raster_boxes(blz_ctx* ctx, const BlzCameraViewData* view, const float* dBoxes, uint32_t boxCount,
+                           float* dDepth, uint32_t width, uint32_t height, blz_stream_t stream);
+
+/* ---------------------------------------------------------------- single-view culls */
+
+typedef struct BlzRenderList {
+    const BlzRenderObject* objects;  /* device; NULL = the scene's default render list */
+    uint32_t count;                  /* drawCount / objCount push constant */
+} BlzRenderList;
+
+typedef struct BlzCullTarget {
+    void* commands;          /* device: records of `stride` bytes */
+    uint32_t stride;         /* BLZ_STRIDE_VULKAN or BLZ_STRIDE_D3D12 */
+    uint32_t capacity;       /* records the buffer can hold */
+    uint32_t* drawCount;     /* device: set to the number of visible records (not accumulated) */
+} BlzCullTarget;
+
+/* Frustum + LOD cull of every object, no occlusion, no visibility state.
+ * Replaces TransparentDrawCull.comp.glsl:13-65 and drawCull.cs.hlsl:10-52 with their dispatch
+ * (DrawCullPass, src/Renderer/BlitzenDX12/dx12Draw.cpp:150-184). view is a host pointer. */
+int blz_cull_frustum(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
+                     const BlzCullTarget* target, blz_stream_t stream);
+
+/* Occlusion pass 1: objects with visibility[i] != 0 are frustum-tested and, when visible, emitted.
+ * visibility is a device uint32 per render object (read only here).
+ * Replaces InitialDrawCull.comp.glsl:12-59 / drawOccFirst.cs.hlsl:13-58 and DrawCullFirstPass
+ * (src/Renderer/BlitzenVulkan/vulkanDraw.cpp:107-158). */
+int blz_cull_first(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
+                   const uint32_t* dVisibility, const BlzCullTarget* target, blz_stream_t stream);
+
+/* Occlusion pass 2: every object is frustum- and Hi-Z-tested against the pyramid; objects visible
+ * now but not last frame are emitted; visibility[i] is rewritten to 1/0.
+ * Replaces LateDrawCull.comp.glsl:13-72 / drawOccLate.cs.hlsl:13-67 and DrawCullOcclusionPass
+ * (src/Renderer/BlitzenVulkan/vulkanDraw.cpp:162-226). */
+int blz_cull_late(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
+                  uint32_t* dVisibility, const BlzPyramid* pyramid, const BlzCullTarget* target,
+                  blz_stream_t stream);
+
+/* Single-pass occlusion against a pyramid (last frame's), no visibility state.
+ * Replaces drawOccTemporal.hlsl:13-64. */
+int blz_cull_temporal(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
+                      const BlzPyramid* pyramid, const BlzCullTarget* target, blz_stream_t stream);
+
+/* Instanced cull: resets counters[l].instanceCount for every LOD, writes each visible object's id
+ * into instances[counters[l].instanceOffset + slot] for its chosen LOD l (slot < slotsPerLod),
+ * then emits one command per LOD with a non-zero count: {objId = instanceOffset, indexCount,
+ * instCount = count, indexOffset = firstIndex, 0, 0}. counters is a device array of the scene's
+ * LOD count; instanceCapacity bounds every write into instances.
+ * Replaces drawInstCountReset.cs.hlsl + drawInstCull.cs.hlsl + drawInstCmd.cs.hlsl and
+ * DrawInstanceCullPass (src/Renderer/BlitzenDX12/dx12Draw.cpp:340-415). */
+int blz_cull_instanced(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
+                       BlzLodInstanceCounter* dCounters, uint32_t* dInstances, uint32_t instanceCapacity,
+                       uint32_t slotsPerLod, const BlzCullTarget* target, blz_stream_t stream);
+
+/* Cluster cull: object frustum + LOD select, then for every cluster of the chosen LOD a sphere
+ * frustum test, a Hi-Z test (when pyramid != NULL) and a normal-cone backface test. Each surviving
+ * cluster emits {objectId, triangleCount*3, 1, dataOffset, 0, 0} and, when dClusterIds != NULL,
+ * its global cluster index into dClusterIds (same slot). Replaces PreClusterDrawCull.comp.glsl
+ * + InitialClusterCull.comp.glsl and the CPU read-back between them
+ * (src/Renderer/BlitzenVulkan/vulkanDraw.cpp:318-423,874-905). */
+int blz_cull_clusters(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
+                      const BlzPyramid* pyramid, const BlzCullTarget* target, uint32_t* dClusterIds,
+                      blz_stream_t stream);
+
+/* ---------------------------------------------------------------- batched views */
+
+#define BLZ_MODE_FRUSTUM 0u
+#define BLZ_MODE_FIRST 1u
+#define BLZ_MODE_LATE 2u
+#define BLZ_MODE_TEMPORAL 3u
+
+typedef struct BlzBatchView {
+    BlzCameraViewData view;          /* the view's cull uniform */
+    BlzRenderList list;              /* its render objects */
+    uint32_t mode;                   /* BLZ_MODE_* */
+    uint32_t reserved0;
+    uint32_t* visibility;            /* device; FIRST and LATE */
+    const BlzPyramid* pyramid;       /* host descriptor; LATE and TEMPORAL */
+    BlzCullTarget target;
+    const BlzMeshTransform* dynamicTransforms; /* device; overrides transforms[0, dynamicCount) */
+    uint32_t dynamicCount;
+    uint32_t reserved1;
+} BlzBatchView;
+
+/* Culls many views of uneven size in one persistent launch: a device work queue of
+ * (view, object tile) items, per-view stable compaction. The reference has one camera and one
+ * dispatch per pass (src/Core/blitzenEngine.h:49); this is the many-view form of the same passes. */
+int blz_cull_batch(blz_ctx* ctx, const BlzBatchView* views, uint32_t viewCount, blz_stream_t stream);
+
+/* Same work as blz_cull_batch, as one dispatch per view (the baseline the batch is compared to). */
+int blz_cull_batch_per_view(blz_ctx* ctx, const BlzBatchView* views, uint32_t viewCount, blz_stream_t stream);
+
+/* Captures blz_cull_batch for a fixed set of views into a CUDA graph and replays it. The views'
+ * buffers must stay valid for the life of the graph; view data may be changed between replays
+ * with blz_batch_graph_set_view. */
+int blz_batch_graph_create(blz_ctx* ctx, const BlzBatchView* views, uint32_t viewCount,
+                           blz_stream_t stream, blz_batch_graph** outGraph);
+int blz_batch_graph_set_view(blz_batch_graph* g, uint32_t viewIndex, const BlzCameraViewData* view);
+int blz_batch_graph_launch(blz_batch_graph* g, blz_stream_t stream);
+int blz_batch_graph_destroy(blz_batch_graph* g);
+
+/* Launch shape used by the batch kernel (threads per block, objects per thread, blocks per SM).
+ * blz_autotune measures the candidate shapes on the given batch and keeps the fastest. */
+typedef struct BlzLaunchShape {
+    uint32_t threadsPerBlock;
+    uint32_t objectsPerThread;
+    uint32_t blocksPerSm;
+    uint32_t reserved;
+} BlzLaunchShape;
+int blz_get_launch_shape(const blz_ctx* ctx, BlzLaunchShape* out);
+int blz_set_launch_shape(blz_ctx* ctx, const BlzLaunchShape* shape);
+int blz_autotune_batch(blz_ctx* ctx, const BlzBatchView* views, uint32_t viewCount, uint32_t repeats,
+                       blz_stream_t stream, BlzLaunchShape* best, float* bestMicroseconds);
+
+/* ---------------------------------------------------------------- serving loop */
+
+typedef struct BlzServeConfig {
+    uint64_t outputPoolBytes;   /* device memory for request outputs; 0 = a quarter of free memory */
+    uint32_t maxInFlight;       /* batches on the device at once (streams) */
+    uint32_t maxBatchViews;     /* requests per batch */
+    uint32_t dynamicCount;      /* transforms [0, dynamicCount) are per-request */
+    uint32_t stride;            /* record stride for request outputs */
+} BlzServeConfig;
+
+typedef struct BlzServeRequest {
+    BlzCameraViewData view;
+    BlzRenderList list;             /* device render list (resident scene) */
+    uint32_t mode;                  /* BLZ_MODE_FRUSTUM or BLZ_MODE_TEMPORAL */
+    uint32_t rotateCount;           /* dynamic objects to rotate for this request (<= dynamicCount) */
+    const BlzPyramid* pyramid;      /* host descriptor, TEMPORAL only */
+    const float* rotateAxes;        /* host, rotateCount unit vectors */
+    float rotateAngle;
+    uint32_t copyToHost;            /* copy records back to host memory on completion */
+} BlzServeRequest;
+
+typedef struct BlzServeResult {
+    uint32_t status;
+    uint32_t drawCount;
+    const void* deviceRecords;      /* device; valid until blz_serve_release */
+    const void* hostRecords;        /* valid until blz_serve_release (copyToHost != 0) */
+    double arrivalSeconds;          /* host monotonic clock */
+    double completeSeconds;
+} BlzServeResult;
+
+typedef struct BlzServeStats {
+    uint64_t submitted, completed, batches, objects;
+    double p50Ms, p99Ms, meanMs, maxMs;
+    uint64_t peakOutputBytes;
+    uint32_t maxConcurrentBatches;
+    uint32_t maxBatchSize;
+} BlzServeStats;
+
+/* A request loop over the resident scene: admits requests as output memory and in-flight slots
+ * free up, batches what is waiting into one batch launch, overlaps batches on several streams. */
+int blz_serve_create(blz_ctx* ctx, const BlzServeConfig* config, blz_server** outServer);
+int blz_serve_submit(blz_server* s, const BlzServeRequest* request, uint64_t* ticketOut);
+int blz_serve_wait(blz_server* s, uint64_t ticket, uint32_t timeoutMs, BlzServeResult* out);
+int blz_serve_release(blz_server* s, uint64_t ticket);
+int blz_serve_stats(blz_server* s, BlzServeStats* out);
+int blz_serve_destroy(blz_server* s);
+
+/* ---------------------------------------------------------------- view constants (host) */
+
+/* Builds the cull uniform the way the reference camera does: view = inverse(T(position) *
+ * R(yaw about -Y) * R(pitch about +X)), infinite reverse-Z projection, symmetric frustum planes,
+ * proj0/proj5, lodTarget = (2 / proj5) / windowHeight.
+ * Restates SetupCamera + UpdateProjection (src/Game/blitzenCamera.cpp:14-41,93-126). fovRadians
+ * is the vertical field of view. */
+int blz_view_setup(BlzCameraViewData* out, float fovRadians, float windowWidth, float windowHeight,
+                   float zNear, float zFar, const float position[3], float yawRadians, float pitchRadians,
+                   float pyramidWidth, float pyramidHeight);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* BLZ_CULL_H */

@@ -1,0 +1,202 @@
+"""Parity of the per-object culls (frustum, occlusion pass 1 / pass 2, temporal) with the oracle.
+
+Bit-exact: draw counts, every record word, and the rewritten visibility buffer.
+"""
+import numpy as np
+import pytest
+import torch
+
+from blitzen_gb300 import abi
+from blitzen_gb300 import scenes as S
+from blitzen_gb300.culler import DevicePyramid, Target, to_device
+from oracle import oracle as O
+from tests.helpers import H, W, assert_records_equal, view_for
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def c1_ctx(lib):
+    from blitzen_gb300.culler import Culler
+    c = Culler(0)
+    sc = S.frustum_lod_scene(100_000, seed=0)
+    c.setup_for_rendering(sc)
+    yield c, sc
+    c.close()
+
+
+@pytest.fixture
+def culler(c1_ctx):
+    return c1_ctx[0]
+
+
+@pytest.fixture
+def c1(c1_ctx):
+    return c1_ctx[1]
+
+
+@pytest.mark.parametrize("zfar", [650.0, 1e30])
+@pytest.mark.parametrize("stride", [abi.STRIDE_VULKAN, abi.STRIDE_D3D12])
+def test_frustum_lod_config1(culler, c1, zfar, stride):
+    v = view_for(zfar=zfar)
+    t = Target.alloc(c1.count, stride)
+    culler.draw_cull(v, t)
+    assert culler.check() == 0
+    gpu = t.read()
+    n, recs, flags = O.cull(0, v, c1, stride=stride)
+    assert flags == 0
+    assert n > 0
+    assert_records_equal(gpu, (n, recs), f"frustum zfar={zfar} stride={stride}")
+
+
+def test_frustum_random_cameras(culler, c1):
+    rng = np.random.default_rng(5)
+    for k in range(6):
+        pos = tuple(float(x) for x in rng.uniform(-800, 800, 3).astype(np.float32))
+        v = view_for(zfar=float(rng.uniform(100, 3000)), position=pos, yaw=float(rng.uniform(-3, 3)),
+                     pitch=float(rng.uniform(-1, 1)))
+        t = Target.alloc(c1.count)
+        culler.draw_cull(v, t)
+        n, recs, _ = O.cull(0, v, c1)
+        assert_records_equal(t.read(), (n, recs), f"camera {k}")
+
+
+def test_capacity_overflow_is_flagged_and_bounded(culler, c1):
+    v = view_for(zfar=1e30)
+    n, recs, _ = O.cull(0, v, c1)
+    cap = n // 2
+    t = Target.alloc(cap + 8)
+    t.capacity = cap
+    sentinel = t.commands.clone()
+    culler.draw_cull(v, t)
+    flags = culler.flags()
+    assert flags & abi.FLAG_COMMAND_OVERFLOW
+    gn, grecs = t.read()
+    assert gn == n
+    assert np.array_equal(grecs[:, :6], recs[:cap, :6])
+    # nothing written past the capacity
+    assert torch.equal(t.commands[cap * 6:], sentinel[cap * 6:])
+
+
+def test_empty_list_writes_zero_count(culler, c1):
+    v = view_for()
+    t = Target.alloc(16)
+    t.count.fill_(12345)
+    culler.draw_cull(v, t, objects=torch.zeros(2, dtype=torch.int32, device="cuda"), count=0)
+    assert culler.check() == 0
+    assert t.read()[0] == 0
+
+
+def test_custom_render_list_and_bad_index(culler, c1):
+    objs = c1.objects[::3].copy()
+    objs["surfaceId"][7] = 10_000          # out of range surface: skipped and flagged
+    objs["transformId"][11] = 10_000_000   # out of range transform
+    dev = to_device(objs, "cuda")
+    v = view_for(zfar=1e30)
+    t = Target.alloc(len(objs))
+    culler.draw_cull(v, t, objects=dev, count=len(objs))
+    flags = culler.flags()
+    assert flags & abi.FLAG_BAD_INDEX
+    n, recs, oflags = O.cull(0, v, c1, objects=objs)
+    assert oflags & abi.FLAG_BAD_INDEX
+    assert_records_equal(t.read(), (n, recs), "custom list")
+
+
+@pytest.fixture(scope="module")
+def stress_ctx(lib):
+    from blitzen_gb300.culler import Culler
+    c = Culler(0)
+    sc = S.stress_scene(1_000_000, seed=1)
+    c.setup_for_rendering(sc)
+    v = view_for(zfar=1e4)
+    depth = O.depth_raster(v, sc.boxes, W, H)
+    yield c, (sc, v, depth)
+    c.close()
+
+
+@pytest.fixture
+def stress(stress_ctx):
+    return stress_ctx[1]
+
+
+@pytest.fixture
+def sculler(stress_ctx):
+    return stress_ctx[0]
+
+
+@pytest.mark.parametrize("mode", [abi.HIZ_D3D12, abi.HIZ_VULKAN])
+def test_pyramid_matches_oracle(sculler, stress, mode):
+    sc, v, depth = stress
+    p = DevicePyramid(W, H, mode)
+    sculler.generate_depth_pyramid(p, torch.from_numpy(depth).cuda())
+    assert sculler.check() == 0
+    ref = O.pyramid_build(depth, mode)
+    got = p.storage.cpu().numpy()
+    assert p.desc.mipCount == ref.desc.mipCount
+    assert np.array_equal(got.view(np.uint32), ref.data.view(np.uint32))
+
+
+@pytest.mark.parametrize("wh", [(1, 1), (1, 7), (2, 3), (7, 1), (65, 33), (129, 257), (1023, 577), (4097, 130)])
+@pytest.mark.parametrize("mode", [abi.HIZ_D3D12, abi.HIZ_VULKAN])
+def test_pyramid_odd_sizes(sculler, wh, mode):
+    w, h = wh
+    rng = np.random.default_rng(w * 131 + h)
+    depth = rng.random((h, w), dtype=np.float32)
+    depth[rng.random((h, w)) < 0.1] = 0.0
+    p = DevicePyramid(w, h, mode)
+    sculler.generate_depth_pyramid(p, torch.from_numpy(depth).cuda())
+    assert sculler.check() == 0
+    ref = O.pyramid_build(depth, mode)
+    assert np.array_equal(p.storage.cpu().numpy().view(np.uint32), ref.data.view(np.uint32)), (w, h, mode)
+
+
+@pytest.mark.parametrize("hiz", [abi.HIZ_D3D12, abi.HIZ_VULKAN])
+def test_two_pass_occlusion(sculler, stress, hiz):
+    sc, v, depth = stress
+    if hiz == abi.HIZ_VULKAN:
+        pl, _ = abi.pyramid_layout(W, H, hiz)
+        v = view_for(zfar=1e4, pw=float(pl.width), ph=float(pl.height))
+    vis = torch.from_numpy(sc.visibility.view(np.int32).copy()).cuda()
+    t1, t2 = Target.alloc(sc.count), Target.alloc(sc.count)
+    p = DevicePyramid(W, H, hiz)
+    sculler.draw_cull_first_pass(v, vis, t1)
+    sculler.generate_depth_pyramid(p, torch.from_numpy(depth).cuda())
+    sculler.draw_cull_occlusion_pass(v, vis, p, t2)
+    assert sculler.check() == 0
+
+    ovis = sc.visibility.copy()
+    n1, r1, _ = O.cull(O_FIRST, v, sc, vis=ovis)
+    opyr = O.pyramid_build(depth, hiz)
+    n2, r2, _ = O.cull(O_LATE, v, sc, vis=ovis, pyramid=opyr)
+    assert_records_equal(t1.read(), (n1, r1), "first pass")
+    assert_records_equal(t2.read(), (n2, r2), "late pass")
+    assert np.array_equal(vis.cpu().numpy().view(np.uint32), ovis)
+    assert n2 > 0 and n1 > 0
+
+
+def test_temporal(sculler, stress):
+    sc, v, depth = stress
+    p = DevicePyramid(W, H)
+    sculler.generate_depth_pyramid(p, torch.from_numpy(depth).cuda())
+    t = Target.alloc(sc.count, abi.STRIDE_D3D12)
+    sculler.draw_cull_temporal(v, p, t)
+    assert sculler.check() == 0
+    n, recs, _ = O.cull(O_TEMPORAL, v, sc, pyramid=O.pyramid_build(depth), stride=abi.STRIDE_D3D12)
+    nf, _, _ = O.cull(0, v, sc)
+    assert 0 < n < nf  # the occluders hide part of the frustum-visible set
+    assert_records_equal(t.read(), (n, recs), "temporal")
+
+
+def test_deterministic_rerun(sculler, stress):
+    sc, v, depth = stress
+    p = DevicePyramid(W, H)
+    sculler.generate_depth_pyramid(p, torch.from_numpy(depth).cuda())
+    outs = []
+    for _ in range(3):
+        t = Target.alloc(sc.count)
+        sculler.draw_cull_temporal(v, p, t)
+        outs.append(t.commands.clone())
+    assert torch.equal(outs[0], outs[1]) and torch.equal(outs[1], outs[2])
+
+
+O_FIRST, O_LATE, O_TEMPORAL = 1, 2, 3

@@ -1,0 +1,319 @@
+"""Parity of the instanced, cluster, raster, transform, batched and serving paths with the oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from blitzen_gb300 import abi
+from blitzen_gb300 import scenes as S
+from blitzen_gb300.abi import BatchView, RenderList
+from blitzen_gb300.culler import Culler, DevicePyramid, Target, to_device
+from oracle import oracle as O
+from tests.helpers import H, W, assert_records_equal, view_for
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def stress_ctx(lib):
+    c = Culler(0)
+    sc = S.stress_scene(300_000, seed=11, extent=3000.0)
+    c.setup_for_rendering(sc)
+    yield c, sc
+    c.close()
+
+
+# ----------------------------------------------------------------------------- instanced
+
+@pytest.mark.parametrize("slots", [100_000, 50])
+def test_instanced_matches_oracle(stress_ctx, slots):
+    c, sc = stress_ctx
+    v = view_for(zfar=1e4)
+    ctr = O.new_counters(sc, slots)
+    cap = len(sc.lods) * slots
+    dctr = torch.from_numpy(ctr.view(np.int32).reshape(-1).copy()).cuda()
+    dinst = torch.full((cap,), -1, dtype=torch.int32, device="cuda")
+    t = Target.alloc(len(sc.lods), abi.STRIDE_D3D12)
+    c.draw_instance_cull_pass(v, dctr, dinst, slots, t)
+    flags = c.flags()
+    n, cmds, octr, oinst, oflags = O.cull_instanced(v, sc, ctr, cap, slots, stride=abi.STRIDE_D3D12)
+    assert flags == oflags
+    if slots == 50:
+        assert flags & abi.FLAG_INSTANCE_OVERFLOW
+    assert_records_equal(t.read(), (n, cmds), "instanced commands")
+    assert np.array_equal(dctr.cpu().numpy().view(np.uint32), octr.view(np.uint32).reshape(-1))
+    assert np.array_equal(dinst.cpu().numpy().view(np.uint32), oinst)
+
+
+def test_instanced_empty_view(stress_ctx):
+    c, sc = stress_ctx
+    v = view_for(zfar=1e4, position=(0.0, 0.0, 1e7))  # every object behind the camera
+    ctr = O.new_counters(sc, 1000)
+    dctr = torch.from_numpy(ctr.view(np.int32).reshape(-1).copy()).cuda()
+    dinst = torch.zeros(len(sc.lods) * 1000, dtype=torch.int32, device="cuda")
+    t = Target.alloc(len(sc.lods))
+    t.count.fill_(77)
+    c.draw_instance_cull_pass(v, dctr, dinst, 1000, t)
+    assert c.check() == 0
+    assert t.read()[0] == 0
+    assert (dctr.cpu().numpy().view(np.uint32).reshape(-1, 2)[:, 1] == 0).all()
+
+
+# ----------------------------------------------------------------------------- raster + transforms
+
+def test_depth_raster_matches_oracle(stress_ctx):
+    c, sc = stress_ctx
+    for k, (pos, yaw) in enumerate([((0.0, 0.0, 0.0), 0.0), ((100.0, -50.0, 200.0), 0.4)]):
+        v = view_for(position=pos, yaw=yaw)
+        depth = torch.full((W * H,), 5.0, dtype=torch.float32, device="cuda")
+        c.raster_boxes(v, torch.from_numpy(sc.boxes.reshape(-1)).cuda(), depth, W, H)
+        assert c.check() == 0
+        ref = O.depth_raster(v, sc.boxes, W, H)
+        assert np.array_equal(depth.cpu().numpy().reshape(H, W), ref), k
+
+
+def test_transforms_update_and_rotate(stress_ctx):
+    c, sc = stress_ctx
+    rng = np.random.default_rng(3)
+    ids = rng.choice(sc.count, 500, replace=False).astype(np.uint32)
+    axes = rng.normal(size=(500, 3))
+    axes = (axes / np.linalg.norm(axes, axis=1, keepdims=True)).astype(np.float32)
+    dst = torch.zeros(500 * 8, dtype=torch.float32, device="cuda")
+    c.rotate_transforms(torch.from_numpy(ids.view(np.int32).copy()).cuda(), torch.from_numpy(axes.reshape(-1)).cuda(),
+                        0.01, dst)
+    assert c.check() == 0
+    ref = O.transforms_rotate(sc.transforms, ids, axes, 0.01)
+    assert np.array_equal(dst.cpu().numpy().view(np.uint32), ref.view(np.uint32).reshape(-1))
+    # scatter them back through the host-array entry point and cull: same as the oracle on the edited scene
+    c.update_object_transform(ids, ref)
+    edited = S.Scene(sc.objects, sc.transforms.copy(), sc.surfaces, sc.lods)
+    edited.transforms[ids] = ref
+    v = view_for(zfar=1e4)
+    t = Target.alloc(sc.count)
+    c.draw_cull(v, t)
+    assert c.check() == 0
+    n, recs, _ = O.cull(0, v, edited)
+    assert_records_equal(t.read(), (n, recs), "after transform update")
+    c.update_object_transform(ids, sc.transforms[ids])  # restore the resident scene
+
+
+# ----------------------------------------------------------------------------- clusters
+
+@pytest.fixture(scope="module")
+def cluster_ctx(lib):
+    c = Culler(0)
+    sc = S.cluster_scene(20_000, seed=2, clusters_per_mesh=200)
+    c.setup_for_rendering(sc)
+    yield c, sc
+    c.close()
+
+
+@pytest.mark.parametrize("with_hiz", [False, True])
+def test_clusters_match_oracle(cluster_ctx, with_hiz):
+    c, sc = cluster_ctx
+    v = view_for(zfar=1e4, position=(0.0, 0.0, -50.0))
+    pyr = opyr = None
+    if with_hiz:
+        depth = O.depth_raster(v, sc.boxes, W, H)
+        pyr = DevicePyramid(W, H)
+        c.generate_depth_pyramid(pyr, torch.from_numpy(depth).cuda())
+        opyr = O.pyramid_build(depth)
+    cap = O._cluster_upper_bound(sc, sc.objects)
+    t = Target.alloc(cap)
+    ids = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    c.cluster_cull(v, t, pyramid=pyr, cluster_ids=ids)
+    assert c.check() == 0
+    n, recs, oids, _ = O.cull_clusters(v, sc, pyramid=opyr, capacity=cap)
+    assert n > 0
+    assert_records_equal(t.read(), (n, recs), "clusters")
+    assert np.array_equal(ids[:n].cpu().numpy().view(np.uint32), oids)
+
+
+def test_cluster_cone_test_culls_something(cluster_ctx):
+    c, sc = cluster_ctx
+    v = view_for(zfar=1e4, position=(0.0, 0.0, -50.0))
+    cap = O._cluster_upper_bound(sc, sc.objects)
+    n, _, _, _ = O.cull_clusters(v, sc, capacity=cap)
+    # all clusters of frustum-visible objects, no cone test: an upper bound the cone test must undercut
+    open_cones = S.Scene(sc.objects, sc.transforms, sc.surfaces, sc.lods, clusters=sc.clusters.copy())
+    open_cones.clusters["coneCutoff"] = 127
+    n_open, _, _, _ = O.cull_clusters(v, open_cones, capacity=cap)
+    assert n < n_open
+
+
+# ----------------------------------------------------------------------------- batch
+
+def _batch(c, sc, n_views=12, seed=4, mode=abi.MODE_TEMPORAL):
+    specs = S.multiview_specs(sc.count, n_views, seed=seed, lo=100, hi=sc.count, extent=1000.0)
+    keep, views, ref = [], (BatchView * n_views)(), []
+    rng = np.random.default_rng(seed)
+    for i, sp in enumerate(specs):
+        v = view_for(zfar=1e4, position=sp.position, yaw=sp.yaw, pitch=sp.pitch)
+        objs = S.subset_objects(sc, sp.subset)
+        dobjs = to_device(objs, "cuda")
+        boxes = S.make_occluders(rng, 300, zmin=50.0, zmax=2000.0)
+        depth = O.depth_raster(view_for(), boxes, W, H)  # any depth image works for parity
+        pyr = DevicePyramid(W, H)
+        c.generate_depth_pyramid(pyr, torch.from_numpy(depth).cuda())
+        t = Target.alloc(len(objs))
+        keep += [dobjs, pyr, t]
+        views[i].view = v
+        views[i].list = RenderList(dobjs.data_ptr(), len(objs))
+        views[i].mode = mode
+        views[i].pyramid = C.pointer(pyr.desc)
+        views[i].target = t.ctype()
+        ref.append((v, objs, O.pyramid_build(depth), t))
+    return views, keep, ref
+
+
+@pytest.mark.parametrize("shape", [(256, 4, 0), (128, 1, 1), (512, 2, 0), (128, 8, 0), (256, 2, 2)])
+def test_batch_matches_per_view_and_oracle(stress_ctx, shape):
+    c, sc = stress_ctx
+    views, keep, ref = _batch(c, sc)
+    lib = abi.load()
+    abi.check(lib.blz_set_launch_shape(c.ctx, C.byref(abi.LaunchShape(shape[0], shape[1], shape[2], 0))), "shape")
+    abi.check(lib.blz_cull_batch(c.ctx, views, len(ref), None), "blz_cull_batch")
+    assert c.check() == 0
+    batched = [r[3].read() for r in ref]
+    for r in ref:
+        r[3].count.fill_(0)
+        r[3].commands.zero_()
+    abi.check(lib.blz_cull_batch_per_view(c.ctx, views, len(ref), None), "per view")
+    assert c.check() == 0
+    for i, (v, objs, opyr, t) in enumerate(ref):
+        per = t.read()
+        assert_records_equal(batched[i], per, f"view {i} batched vs per-view")
+        n, recs, _ = O.cull(3, v, sc, objects=objs, pyramid=opyr)
+        assert_records_equal(batched[i], (n, recs), f"view {i} vs oracle")
+
+
+def test_batch_graph_replay(stress_ctx):
+    c, sc = stress_ctx
+    views, keep, ref = _batch(c, sc, n_views=8, seed=9)
+    lib = abi.load()
+    g = C.c_void_p()
+    abi.check(lib.blz_batch_graph_create(c.ctx, views, len(ref), None, C.byref(g)), "graph create")
+    try:
+        for rep in range(3):
+            for r in ref:
+                r[3].count.fill_(0)
+            abi.check(lib.blz_batch_graph_launch(g, None), "graph launch")
+            assert c.check() == 0
+            for i, (v, objs, opyr, t) in enumerate(ref):
+                n, recs, _ = O.cull(3, v, sc, objects=objs, pyramid=opyr)
+                assert_records_equal(t.read(), (n, recs), f"replay {rep} view {i}")
+        # a new camera for view 0 between replays
+        nv = view_for(zfar=1e4, yaw=1.0)
+        abi.check(lib.blz_batch_graph_set_view(g, 0, C.byref(nv)), "set view")
+        abi.check(lib.blz_batch_graph_launch(g, None), "graph launch")
+        assert c.check() == 0
+        n, recs, _ = O.cull(3, nv, sc, objects=ref[0][1], pyramid=ref[0][2])
+        assert_records_equal(ref[0][3].read(), (n, recs), "view 0 after set_view")
+    finally:
+        lib.blz_batch_graph_destroy(g)
+
+
+def test_autotune_picks_a_supported_shape(stress_ctx):
+    c, sc = stress_ctx
+    views, keep, ref = _batch(c, sc, n_views=4, seed=21)
+    lib = abi.load()
+    best, us = abi.LaunchShape(), C.c_float(0)
+    abi.check(lib.blz_autotune_batch(c.ctx, views, len(ref), 2, None, C.byref(best), C.byref(us)), "autotune")
+    assert best.threadsPerBlock in (128, 256, 512) and best.objectsPerThread in (1, 2, 4, 8)
+    assert us.value > 0
+
+
+# ----------------------------------------------------------------------------- serving
+
+def _serve_requests(sc, n, seed):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(n):
+        count = int(np.exp(rng.uniform(np.log(1000), np.log(sc.count // 2))))
+        start = int(rng.integers(0, sc.count - count))
+        axes = rng.normal(size=(1000, 3))
+        axes = (axes / np.linalg.norm(axes, axis=1, keepdims=True)).astype(np.float32)
+        pos = tuple(float(x) for x in rng.uniform(-500, 500, 3).astype(np.float32))
+        reqs.append((start, count, axes, view_for(zfar=1e4, position=pos, yaw=float(rng.uniform(-3, 3)))))
+    return reqs
+
+
+def _submit(lib, server, c, reqs):
+    objs_dev = c.scene_tensors[0]
+    tickets = []
+    for start, count, axes, v in reqs:
+        r = abi.ServeRequest()
+        r.view = v
+        r.list = RenderList(objs_dev.data_ptr() + start * 8, count)
+        r.mode = abi.MODE_FRUSTUM
+        r.rotateCount = 1000
+        r.rotateAxes = axes.ctypes.data
+        r.rotateAngle = 0.01
+        r.copyToHost = 1
+        t = C.c_uint64()
+        abi.check(lib.blz_serve_submit(server, C.byref(r), C.byref(t)), "submit")
+        tickets.append(t.value)
+    return tickets
+
+
+def _collect(lib, server, tickets):
+    out = []
+    for t in tickets:
+        res = abi.ServeResult()
+        abi.check(lib.blz_serve_wait(server, t, 20_000, C.byref(res)), "wait")
+        n = res.drawCount
+        recs = np.ctypeslib.as_array(C.cast(res.hostRecords, C.POINTER(C.c_uint32)), shape=(n * 6,)).copy() if n else np.zeros(0, np.uint32)
+        out.append((res.status, n, recs))
+        abi.check(lib.blz_serve_release(server, t), "release")
+    return out
+
+
+def test_serving_results_same_alone_and_in_the_mix(stress_ctx):
+    c, sc = stress_ctx
+    lib = abi.load()
+    cfg = abi.ServeConfig(256 << 20, 4, 16, 1000, abi.STRIDE_VULKAN)
+    server = C.c_void_p()
+    abi.check(lib.blz_serve_create(c.ctx, C.byref(cfg), C.byref(server)), "serve create")
+    try:
+        reqs = _serve_requests(sc, 24, seed=1)
+        alone = []
+        for rq in reqs:
+            alone += _collect(lib, server, _submit(lib, server, c, [rq]))
+        mixed = _collect(lib, server, _submit(lib, server, c, reqs))
+        stats = abi.ServeStats()
+        lib.blz_serve_stats(server, C.byref(stats))
+        assert stats.completed == 48
+        assert stats.maxBatchSize > 1  # the mix was batched
+        for k, (a, m) in enumerate(zip(alone, mixed)):
+            assert a[0] == 0 and m[0] == 0
+            assert a[1] == m[1] and np.array_equal(a[2], m[2]), f"request {k} differs alone vs mixed"
+        # one request against the oracle with its rotated dynamic objects applied
+        start, count, axes, v = reqs[3]
+        rot = O.transforms_rotate(sc.transforms, np.arange(1000, dtype=np.uint32), axes, 0.01)
+        edited = S.Scene(sc.objects, sc.transforms.copy(), sc.surfaces, sc.lods)
+        edited.transforms[:1000] = rot
+        n, recs, _ = O.cull(0, v, edited, objects=sc.objects[start:start + count])
+        assert alone[3][1] == n
+        assert np.array_equal(alone[3][2].reshape(-1, 6), recs[:, :6])
+    finally:
+        lib.blz_serve_destroy(server)
+
+
+def test_serving_admission_waits_for_memory(stress_ctx):
+    c, sc = stress_ctx
+    lib = abi.load()
+    # a pool that holds about one large request at a time
+    cfg = abi.ServeConfig(8 << 20, 4, 16, 1000, abi.STRIDE_VULKAN)
+    server = C.c_void_p()
+    abi.check(lib.blz_serve_create(c.ctx, C.byref(cfg), C.byref(server)), "serve create")
+    try:
+        reqs = [(0, 250_000, np.tile(np.float32([0, 0, 1]), (1000, 1)), view_for(zfar=1e4))] * 6
+        res = _collect(lib, server, _submit(lib, server, c, reqs))
+        assert all(r[0] == 0 for r in res)
+        assert len({r[1] for r in res}) == 1
+        stats = abi.ServeStats()
+        lib.blz_serve_stats(server, C.byref(stats))
+        assert stats.peakOutputBytes <= 8 << 20
+    finally:
+        lib.blz_serve_destroy(server)
