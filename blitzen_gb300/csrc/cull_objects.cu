@@ -48,14 +48,35 @@ __device__ __forceinline__ uint32_t find_view(const uint32_t* tileStart, uint32_
 
 // ------------------------------------------------------------------ decisions
 
-// Frustum (+ Hi-Z for LATE/TEMPORAL) and LOD of the OPT objects a thread owns in a chunk
-// (object base + k * THREADS + lane). Loads are issued in phases — visibility, render objects,
-// transforms — before any arithmetic or store, so each thread keeps all its DRAM reads in flight at
-// once; surface and LOD rows (small tables, L1 resident) are read in the compute phase.
+// Per-block shared memory of the decide kernel: the queue of frustum survivors of a chunk (their
+// view-space spheres and LOD ranges) and the per-object results the queue work hands back.
+template <int CHUNK>
+struct DecideSmem {
+    float qx[CHUNK], qy[CHUNK], qz[CHUNK], qr[CHUNK], qs[CHUNK];
+    uint32_t qidx[CHUNK];      // object index in the chunk | want-emit flag in bit 31
+    uint32_t qlodOff[CHUNK];   // the surface's LOD range
+    uint32_t qlodCnt[CHUNK];
+    uint32_t result[CHUNK];    // per object: lodId if emitted, kNotEmitted otherwise
+    uint8_t visible[CHUNK];    // per object: final visibility (LATE rewrites the buffer with it)
+    uint32_t queueLen;
+};
+
+constexpr uint32_t kNotEmitted = 0xFFFFFFFFu;
+
+// Decisions of one chunk in three phases:
+//   A  every thread loads its OPT objects (render object, then transform — all reads issued before
+//      any arithmetic) and runs the frustum test; survivors are appended to a shared queue with one
+//      shared atomic per warp and k;
+//   B  the block walks the queue — the sphere projection, Hi-Z test (LATE/TEMPORAL) and LOD
+//      selection run on dense lanes instead of on every lane of every warp that has one survivor;
+//   C  every thread reads its objects' results back in object order (the caller ranks them).
 template <int MODE, int THREADS, int OPT>
 __device__ __forceinline__ void decide_chunk(const SceneTables& sc, const BatchViewDev& bv, uint32_t base,
-                                             bool (&emit)[OPT], uint32_t (&lodId)[OPT], unsigned int& flags) {
+                                             DecideSmem<THREADS * OPT>& sm, bool (&emit)[OPT], uint32_t (&lodId)[OPT],
+                                             unsigned int& flags) {
     const uint32_t count = bv.count;
+    const uint32_t lane = threadIdx.x & 31u;
+    if (threadIdx.x == 0) sm.queueLen = 0u;
     uint32_t visPrev[OPT];
     bool act[OPT];
 #pragma unroll
@@ -63,8 +84,6 @@ __device__ __forceinline__ void decide_chunk(const SceneTables& sc, const BatchV
         const uint32_t i = base + k * THREADS + threadIdx.x;
         act[k] = i < count;
         visPrev[k] = 1u;
-        emit[k] = false;
-        lodId[k] = 0u;
         if (MODE == BLZ_MODE_FIRST && act[k]) visPrev[k] = __ldg(bv.vis + i);
         if (MODE == BLZ_MODE_LATE && act[k]) visPrev[k] = bv.vis[i];  // rewritten below: coherent load
     }
@@ -92,46 +111,82 @@ __device__ __forceinline__ void decide_chunk(const SceneTables& sc, const BatchV
             q[k] = __ldg(tp + 1);
         }
     }
+    __syncthreads();  // queueLen reset is visible
     const ViewConsts v = load_view(bv.view);
+    const uint32_t lt = lanemask_lt();
 #pragma unroll
     for (int k = 0; k < OPT; ++k) {
-        if (!act[k]) continue;
-        const uint32_t i = base + k * THREADS + threadIdx.x;
-        bool visible = false;
+        const uint32_t idx = k * THREADS + threadIdx.x;
+        bool inFrustum = false;
         Vec3 c{0.f, 0.f, 0.f};
         float r = 0.f;
         uint4 s1 = make_uint4(0u, 0u, 0u, 0u);
-        bool good = ok[k];
-        if (good) {
+        if (ok[k]) {
             const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + ro[k].y);
             const float4 sph = __ldg(sp);
             s1 = __ldg(reinterpret_cast<const uint4*>(sp + 1));  // materialId, lodOffset, lodCount, vertexOffset
-            good = s1.y < sc.lodCount && s1.z <= sc.lodCount - s1.y;
-            if (good) {
+            if (s1.y < sc.lodCount && s1.z <= sc.lodCount - s1.y) {
                 c = view_transform(v.rows, model_to_world(Vec3{sph.x, sph.y, sph.z}, ps[k], q[k]));
                 r = BLZ_FM(sph.w, ps[k].w);
-                visible = frustum_check(c, r, v);
-                if ((MODE == BLZ_MODE_LATE || MODE == BLZ_MODE_TEMPORAL) && visible) {
-                    float4 aabb;
-                    if (project_sphere(c, r, v.zNear, v.proj0, v.proj5, aabb)) visible = visible && occlusion(aabb, bv.pyr, v, c, r);
-                }
+                inFrustum = frustum_check(c, r, v);
+            } else {
+                flags |= BLZ_FLAG_BAD_INDEX;
             }
+        } else if (act[k]) {
+            flags |= BLZ_FLAG_BAD_INDEX;
         }
-        if (!good) flags |= BLZ_FLAG_BAD_INDEX;
-        bool e = visible;
-        if (MODE == BLZ_MODE_LATE) {
-            e = visible && visPrev[k] == 0u;  // drawOccLate.cs.hlsl:45
-            bv.vis[i] = visible ? 1u : 0u;    // drawOccLate.cs.hlsl:67
+        sm.visible[idx] = 0;
+        sm.result[idx] = kNotEmitted;
+        // append the survivors: one shared atomic per warp
+        const unsigned b = __ballot_sync(0xFFFFFFFFu, inFrustum);
+        uint32_t at = 0;
+        if (lane == 0 && b) at = atomicAdd(&sm.queueLen, static_cast<uint32_t>(__popc(b)));
+        at = __shfl_sync(0xFFFFFFFFu, at, 0) + __popc(b & lt);
+        if (inFrustum) {
+            const bool want = (MODE == BLZ_MODE_LATE) ? (visPrev[k] == 0u) : true;
+            sm.qx[at] = c.x;
+            sm.qy[at] = c.y;
+            sm.qz[at] = c.z;
+            sm.qr[at] = r;
+            sm.qs[at] = ps[k].w;
+            sm.qidx[at] = idx | (want ? 0x80000000u : 0u);
+            sm.qlodOff[at] = s1.y;
+            sm.qlodCnt[at] = s1.z;
         }
-        if (e) {
+    }
+    __syncthreads();
+    // B: dense work over the survivors
+    const uint32_t n = sm.queueLen;
+    for (uint32_t j = threadIdx.x; j < n; j += THREADS) {
+        const Vec3 c{sm.qx[j], sm.qy[j], sm.qz[j]};
+        const float r = sm.qr[j];
+        const uint32_t id = sm.qidx[j];
+        bool visible = true;
+        if (MODE == BLZ_MODE_LATE || MODE == BLZ_MODE_TEMPORAL) {
+            float4 aabb;
+            if (project_sphere(c, r, v.zNear, v.proj0, v.proj5, aabb)) visible = occlusion(aabb, bv.pyr, v, c, r);
+        }
+        const uint32_t idx = id & 0x7FFFFFFFu;
+        sm.visible[idx] = visible ? 1 : 0;
+        if (visible && (id & 0x80000000u)) {
             // cullBuffers.hlsl:42-55 — last LOD in [1, lodCount) with error < threshold
-            const float threshold = lod_threshold(c, r, ps[k].w, v.lodTarget);
+            const uint32_t lodOff = sm.qlodOff[j], lodCnt = sm.qlodCnt[j];
+            const float threshold = lod_threshold(c, r, sm.qs[j], v.lodTarget);
             uint32_t sel = 0;
-            for (uint32_t j = 1; j < s1.z; ++j)
-                if (__ldg(&sc.lods[s1.y + j].error) < threshold) sel = j;
-            lodId[k] = s1.y + sel;
+            for (uint32_t t = 1; t < lodCnt; ++t)
+                if (__ldg(&sc.lods[lodOff + t].error) < threshold) sel = t;
+            sm.result[idx] = lodOff + sel;
         }
-        emit[k] = e;
+    }
+    __syncthreads();
+    // C: results back to the owning threads, in object order
+#pragma unroll
+    for (int k = 0; k < OPT; ++k) {
+        const uint32_t idx = k * THREADS + threadIdx.x;
+        const uint32_t res = sm.result[idx];
+        emit[k] = res != kNotEmitted;
+        lodId[k] = res;
+        if (MODE == BLZ_MODE_LATE && act[k]) bv.vis[base + idx] = sm.visible[idx];  // drawOccLate.cs.hlsl:67
     }
 }
 
@@ -304,6 +359,7 @@ __global__ void __launch_bounds__(THREADS) cull_decide_kernel(const PipeParams p
     __shared__ uint32_t s_off[OPT * NW];
     __shared__ uint32_t s_sum[NW], s_flag[NW];
     __shared__ int s_last;
+    __shared__ DecideSmem<CHUNK> s_dec;
     const uint32_t warp = threadIdx.x >> 5;
     unsigned int flags = 0u;
     for (uint32_t chunk = blockIdx.x; chunk < p.totalTiles; chunk += gridDim.x) {
@@ -318,13 +374,13 @@ __global__ void __launch_bounds__(THREADS) cull_decide_kernel(const PipeParams p
         uint32_t lod[OPT];
         if (MODE == kModeRuntime) {
             switch (bv.mode) {
-                case BLZ_MODE_FIRST: decide_chunk<BLZ_MODE_FIRST, THREADS, OPT>(p.sc, bv, base, emit, lod, flags); break;
-                case BLZ_MODE_LATE: decide_chunk<BLZ_MODE_LATE, THREADS, OPT>(p.sc, bv, base, emit, lod, flags); break;
-                case BLZ_MODE_TEMPORAL: decide_chunk<BLZ_MODE_TEMPORAL, THREADS, OPT>(p.sc, bv, base, emit, lod, flags); break;
-                default: decide_chunk<BLZ_MODE_FRUSTUM, THREADS, OPT>(p.sc, bv, base, emit, lod, flags); break;
+                case BLZ_MODE_FIRST: decide_chunk<BLZ_MODE_FIRST, THREADS, OPT>(p.sc, bv, base, s_dec, emit, lod, flags); break;
+                case BLZ_MODE_LATE: decide_chunk<BLZ_MODE_LATE, THREADS, OPT>(p.sc, bv, base, s_dec, emit, lod, flags); break;
+                case BLZ_MODE_TEMPORAL: decide_chunk<BLZ_MODE_TEMPORAL, THREADS, OPT>(p.sc, bv, base, s_dec, emit, lod, flags); break;
+                default: decide_chunk<BLZ_MODE_FRUSTUM, THREADS, OPT>(p.sc, bv, base, s_dec, emit, lod, flags); break;
             }
         } else {
-            decide_chunk<(MODE < 0 ? 0 : MODE), THREADS, OPT>(p.sc, bv, base, emit, lod, flags);
+            decide_chunk<(MODE < 0 ? 0 : MODE), THREADS, OPT>(p.sc, bv, base, s_dec, emit, lod, flags);
         }
         uint32_t lrank[OPT];
         const uint32_t total = block_rank<THREADS, OPT>(emit, lrank, s_off);
