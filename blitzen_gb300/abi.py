@@ -179,6 +179,10 @@ _PROTOS = {
     "blz_get_launch_shape": (_I, [_P, C.POINTER(LaunchShape)]),
     "blz_set_launch_shape": (_I, [_P, C.POINTER(LaunchShape)]),
     "blz_autotune_batch": (_I, [_P, C.POINTER(BatchView), _U32, _U32, _P, C.POINTER(LaunchShape), C.POINTER(C.c_float)]),
+    "blz_capture_begin": (_I, [_P, _P]),
+    "blz_capture_end": (_I, [_P, _P, C.POINTER(_P), C.POINTER(_U32)]),
+    "blz_graph_launch": (_I, [_P, _P]),
+    "blz_graph_destroy": (_I, [_P]),
     "blz_serve_create": (_I, [_P, C.POINTER(ServeConfig), C.POINTER(_P)]),
     "blz_serve_submit": (_I, [_P, C.POINTER(ServeRequest), C.POINTER(C.c_uint64)]),
     "blz_serve_wait": (_I, [_P, C.c_uint64, _U32, C.POINTER(ServeResult)]),

@@ -93,6 +93,7 @@ int resolve_list(const blz_ctx* c, BlzRenderList list, const BlzRenderObject** o
 int ensure_chunk_scratch(blz_ctx* c, size_t chunks, size_t chunkSize) {
     const size_t objects = chunks * chunkSize;
     if (objects <= c->chunkObjects && chunks <= c->chunkSlots) return BLZ_OK;
+    if (c->capturing) return fail(BLZ_ERR_CAPACITY, "scratch must grow, which a capture cannot record: run the calls once before capturing");
     size_t wantObj = objects > c->chunkObjects ? objects + objects / 4 : c->chunkObjects;
     size_t wantSlots = chunks > c->chunkSlots ? chunks + chunks / 4 + 64 : c->chunkSlots;
     if (c->chunkMem) {
@@ -429,7 +430,7 @@ static int object_cull(blz_ctx* c, uint32_t mode, const BlzCameraViewData* view,
         rc = check_pyramid(pyr, true);
         if (rc != BLZ_OK) return rc;
     }
-    const uint32_t tile = c->single_tile();
+    const uint32_t tile = object_tile_size();
     uint32_t tiles = (count + tile - 1) / tile;
     if (tiles == 0) tiles = 1;  // an empty list still gets one chunk, and its draw count is written
     rc = ensure_chunk_scratch(c, tiles, tile);

@@ -40,10 +40,10 @@ struct blz_ctx {
     uint32_t defaultCount = 0;
     std::vector<void*> ownedScene;
     std::atomic<uint64_t> launches{0};
+    bool capturing = false;            // a blz_capture_begin is open
+    uint64_t launchesAtCapture = 0;
     BlzLaunchShape shape{256, 2, 0, 0};   // batch launches
     uint32_t singleThreads = 256, singleOpt = 2;  // single-view launches
-
-    uint32_t single_tile() const { return singleThreads * singleOpt; }
 };
 
 namespace blz {

@@ -105,7 +105,7 @@ static int ensure_batch_dev(blz_ctx* c, size_t bytes) {
 int run_batch(blz_ctx* c, const BlzBatchView* views, uint32_t n, cudaStream_t st) {
     if (!c || (n && !views)) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or views is NULL");
     if (n == 0) return BLZ_OK;
-    const uint32_t tile = c->shape.threadsPerBlock * c->shape.objectsPerThread;
+    const uint32_t tile = object_tile_size();
     std::vector<BatchViewDev> d;
     std::vector<uint32_t> ts;
     int rc = build_views(c, views, n, tile, d, ts);
@@ -137,7 +137,59 @@ struct blz_batch_graph {
     cudaGraphExec_t exec = nullptr;
 };
 
+struct blz_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint32_t kernels = 0;
+    blz_ctx* ctx = nullptr;
+};
+
 extern "C" {
+
+int blz_capture_begin(blz_ctx* c, blz_stream_t stream) {
+    if (!c || !stream) return fail(BLZ_ERR_INVALID_ARGUMENT, "capture needs a context and a non-default stream");
+    if (c->capturing) return fail(BLZ_ERR_INVALID_ARGUMENT, "a capture is already open on this context");
+    cudaError_t e = cudaStreamBeginCapture(reinterpret_cast<cudaStream_t>(stream), cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
+    c->capturing = true;
+    c->launchesAtCapture = c->launches.load();
+    return BLZ_OK;
+}
+
+int blz_capture_end(blz_ctx* c, blz_stream_t stream, blz_graph** out, uint32_t* kernelsOut) {
+    if (!c || !out) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or out is NULL");
+    *out = nullptr;
+    if (!c->capturing) return fail(BLZ_ERR_INVALID_ARGUMENT, "no capture is open on this context");
+    c->capturing = false;
+    blz_graph* g = new blz_graph();
+    g->ctx = c;
+    g->kernels = static_cast<uint32_t>(c->launches.load() - c->launchesAtCapture);
+    cudaError_t e = cudaStreamEndCapture(reinterpret_cast<cudaStream_t>(stream), &g->graph);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e != cudaSuccess) {
+        blz_graph_destroy(g);
+        return cuda_fail(e, "capture end");
+    }
+    if (kernelsOut) *kernelsOut = g->kernels;
+    *out = g;
+    return BLZ_OK;
+}
+
+int blz_graph_launch(blz_graph* g, blz_stream_t stream) {
+    if (!g || !g->exec) return fail(BLZ_ERR_INVALID_ARGUMENT, "graph is NULL");
+    cudaError_t e = cudaGraphLaunch(g->exec, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+    g->ctx->launches += g->kernels;
+    return BLZ_OK;
+}
+
+int blz_graph_destroy(blz_graph* g) {
+    if (!g) return BLZ_OK;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return BLZ_OK;
+}
 
 int blz_cull_batch(blz_ctx* c, const BlzBatchView* views, uint32_t n, blz_stream_t stream) {
     return run_batch(c, views, n, reinterpret_cast<cudaStream_t>(stream));
@@ -148,11 +200,11 @@ int blz_cull_batch_per_view(blz_ctx* c, const BlzBatchView* views, uint32_t n, b
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     std::vector<BatchViewDev> d;
     std::vector<uint32_t> ts;
-    int rc = build_views(c, views, n, c->single_tile(), d, ts);
+    int rc = build_views(c, views, n, object_tile_size(), d, ts);
     if (rc != BLZ_OK) return rc;
     uint32_t maxTiles = 1;
     for (uint32_t i = 0; i < n; ++i) maxTiles = std::max(maxTiles, ts[i + 1] - ts[i]);
-    rc = ensure_chunk_scratch(c, maxTiles, c->single_tile());
+    rc = ensure_chunk_scratch(c, maxTiles, object_tile_size());
     if (rc != BLZ_OK) return rc;
     for (uint32_t i = 0; i < n; ++i) {
         PipeParams p{};
@@ -233,7 +285,7 @@ int blz_batch_graph_create(blz_ctx* c, const BlzBatchView* views, uint32_t n, bl
     if (!c || !views || n == 0 || !outGraph) return fail(BLZ_ERR_INVALID_ARGUMENT, "bad batch graph arguments");
     *outGraph = nullptr;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const uint32_t tile = c->shape.threadsPerBlock * c->shape.objectsPerThread;
+    const uint32_t tile = object_tile_size();
     std::vector<BatchViewDev> d;
     std::vector<uint32_t> ts;
     int rc = build_views(c, views, n, tile, d, ts);

@@ -48,146 +48,157 @@ __device__ __forceinline__ uint32_t find_view(const uint32_t* tileStart, uint32_
 
 // ------------------------------------------------------------------ decisions
 
-// Per-block shared memory of the decide kernel: the queue of frustum survivors of a chunk (their
-// view-space spheres and LOD ranges) and the per-object results the queue work hands back.
-template <int CHUNK>
-struct DecideSmem {
-    float qx[CHUNK], qy[CHUNK], qz[CHUNK], qr[CHUNK], qs[CHUNK];
-    uint32_t qidx[CHUNK];      // object index in the chunk | want-emit flag in bit 31
-    uint32_t qlodOff[CHUNK];   // the surface's LOD range
-    uint32_t qlodCnt[CHUNK];
-    uint32_t result[CHUNK];    // per object: lodId if emitted, kNotEmitted otherwise
-    uint8_t visible[CHUNK];    // per object: final visibility (LATE rewrites the buffer with it)
-    uint32_t queueLen;
-};
+constexpr uint32_t kChunk = 512;  // objects per chunk: the unit of staging, counting and scanning
 
-constexpr uint32_t kNotEmitted = 0xFFFFFFFFu;
-
-// Decisions of one chunk in three phases:
-//   A  every thread loads its OPT objects (render object, then transform — all reads issued before
-//      any arithmetic) and runs the frustum test; survivors are appended to a shared queue with one
-//      shared atomic per warp and k;
-//   B  the block walks the queue — the sphere projection, Hi-Z test (LATE/TEMPORAL) and LOD
-//      selection run on dense lanes instead of on every lane of every warp that has one survivor;
-//   C  every thread reads its objects' results back in object order (the caller ranks them).
-template <int MODE, int THREADS, int OPT>
-__device__ __forceinline__ void decide_chunk(const SceneTables& sc, const BatchViewDev& bv, uint32_t base,
-                                             DecideSmem<THREADS * OPT>& sm, bool (&emit)[OPT], uint32_t (&lodId)[OPT],
-                                             unsigned int& flags) {
-    const uint32_t count = bv.count;
+// One warp decides a chunk of kChunk consecutive render objects of a view, 32 * OPT at a time
+// (object base + k * 32 + lane for k < OPT, so the step is k-major and lanes ascend).
+// For each step:
+//   1  every lane loads its OPT render objects and then their transforms (all reads issued before
+//      any arithmetic) and runs the frustum test;
+//   2  the frustum survivors are ranked with ballots — survivor order is object order — and handed
+//      to dense lanes with __fns + shuffles, so the sphere projection, Hi-Z test (LATE/TEMPORAL)
+//      and LOD selection run on packed lanes, not on every lane of every warp with a survivor;
+//   3  the emitted survivors are ranked with one more ballot and appended to the chunk's staging
+//      as (objectId, lodId); LATE writes every object's new visibility.
+// No shared memory and no block barrier: warps never wait for one another.
+template <int MODE, int OPT>
+__device__ __forceinline__ uint32_t decide_chunk_warp(const SceneTables& sc, const BatchViewDev& bv, uint32_t base,
+                                                      uint2* stage, unsigned int& flags) {
+    constexpr uint32_t STEP = 32u * OPT;
     const uint32_t lane = threadIdx.x & 31u;
-    if (threadIdx.x == 0) sm.queueLen = 0u;
-    uint32_t visPrev[OPT];
-    bool act[OPT];
-#pragma unroll
-    for (int k = 0; k < OPT; ++k) {
-        const uint32_t i = base + k * THREADS + threadIdx.x;
-        act[k] = i < count;
-        visPrev[k] = 1u;
-        if (MODE == BLZ_MODE_FIRST && act[k]) visPrev[k] = __ldg(bv.vis + i);
-        if (MODE == BLZ_MODE_LATE && act[k]) visPrev[k] = bv.vis[i];  // rewritten below: coherent load
-    }
-    if (MODE == BLZ_MODE_FIRST) {
-#pragma unroll
-        for (int k = 0; k < OPT; ++k) act[k] = act[k] && visPrev[k] != 0u;  // drawOccFirst.cs.hlsl:22-25
-    }
-    uint2 ro[OPT];
-#pragma unroll
-    for (int k = 0; k < OPT; ++k) {
-        ro[k] = make_uint2(0u, 0u);
-        if (act[k]) ro[k] = __ldg(reinterpret_cast<const uint2*>(bv.objects) + base + k * THREADS + threadIdx.x);
-    }
-    float4 ps[OPT], q[OPT];
-    bool ok[OPT];
-#pragma unroll
-    for (int k = 0; k < OPT; ++k) {
-        ok[k] = act[k] && ro[k].x < sc.transformCount && ro[k].y < sc.surfaceCount;
-        ps[k] = make_float4(0.f, 0.f, 0.f, 1.f);
-        q[k] = make_float4(0.f, 0.f, 0.f, 1.f);
-        if (ok[k]) {
-            const BlzMeshTransform* t = ((bv.dynT != nullptr && ro[k].x < bv.dynCount) ? bv.dynT : sc.transforms) + ro[k].x;
-            const float4* tp = reinterpret_cast<const float4*>(t);
-            ps[k] = __ldg(tp);
-            q[k] = __ldg(tp + 1);
-        }
-    }
-    __syncthreads();  // queueLen reset is visible
+    const uint32_t count = bv.count;
     const ViewConsts v = load_view(bv.view);
-    const uint32_t lt = lanemask_lt();
+    uint32_t run = 0;  // emitted so far in this chunk
+    const uint32_t limit = min(base + kChunk, count);
+    // render objects and visibility words of the next step are fetched one step ahead, so a step
+    // waits on one DRAM latency (its transforms), not two
+    uint2 nro[OPT];
+    uint32_t nvis[OPT];
+    auto prefetch = [&](uint32_t at) {
 #pragma unroll
-    for (int k = 0; k < OPT; ++k) {
-        const uint32_t idx = k * THREADS + threadIdx.x;
-        bool inFrustum = false;
-        Vec3 c{0.f, 0.f, 0.f};
-        float r = 0.f;
-        uint4 s1 = make_uint4(0u, 0u, 0u, 0u);
-        if (ok[k]) {
-            const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + ro[k].y);
-            const float4 sph = __ldg(sp);
-            s1 = __ldg(reinterpret_cast<const uint4*>(sp + 1));  // materialId, lodOffset, lodCount, vertexOffset
-            if (s1.y < sc.lodCount && s1.z <= sc.lodCount - s1.y) {
-                c = view_transform(v.rows, model_to_world(Vec3{sph.x, sph.y, sph.z}, ps[k], q[k]));
-                r = BLZ_FM(sph.w, ps[k].w);
-                inFrustum = frustum_check(c, r, v);
-            } else {
+        for (int k = 0; k < OPT; ++k) {
+            const uint32_t i = at + k * 32u + lane;
+            const bool in = i < limit;
+            nro[k] = in ? __ldg(reinterpret_cast<const uint2*>(bv.objects) + i) : make_uint2(0u, 0u);
+            nvis[k] = 1u;
+            if (MODE == BLZ_MODE_FIRST && in) nvis[k] = __ldg(bv.vis + i);
+            if (MODE == BLZ_MODE_LATE && in) nvis[k] = bv.vis[i];  // rewritten later by this warp: coherent load
+        }
+    };
+    prefetch(base);
+    for (uint32_t sb = base; sb < limit; sb += STEP) {
+        // 1. loads, then the frustum test on the owning lane
+        uint32_t visPrev[OPT];
+        bool act[OPT];
+        uint2 ro[OPT];
+#pragma unroll
+        for (int k = 0; k < OPT; ++k) {
+            const uint32_t i = sb + k * 32u + lane;
+            act[k] = i < limit;
+            visPrev[k] = nvis[k];
+            if (MODE == BLZ_MODE_FIRST) act[k] = act[k] && visPrev[k] != 0u;  // drawOccFirst.cs.hlsl:22-25
+            ro[k] = act[k] ? nro[k] : make_uint2(0u, 0u);
+        }
+        float4 ps[OPT], q[OPT];
+        bool ok[OPT];
+#pragma unroll
+        for (int k = 0; k < OPT; ++k) {
+            ok[k] = act[k] && ro[k].x < sc.transformCount && ro[k].y < sc.surfaceCount;
+            ps[k] = make_float4(0.f, 0.f, 0.f, 1.f);
+            q[k] = make_float4(0.f, 0.f, 0.f, 1.f);
+            if (ok[k]) {
+                const BlzMeshTransform* t = ((bv.dynT != nullptr && ro[k].x < bv.dynCount) ? bv.dynT : sc.transforms) + ro[k].x;
+                const float4* tp = reinterpret_cast<const float4*>(t);
+                ps[k] = __ldg(tp);
+                q[k] = __ldg(tp + 1);
+            }
+        }
+        if (sb + STEP < limit) prefetch(sb + STEP);
+        float cx[OPT], cy[OPT], cz[OPT], cr[OPT];
+        uint32_t lodOff[OPT], lodCnt[OPT];
+        unsigned survivors[OPT];
+        uint32_t before[OPT + 1];
+        before[0] = 0;
+#pragma unroll
+        for (int k = 0; k < OPT; ++k) {
+            bool inFrustum = false;
+            cx[k] = cy[k] = cz[k] = cr[k] = 0.f;
+            lodOff[k] = lodCnt[k] = 0u;
+            if (ok[k]) {
+                const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + ro[k].y);
+                const float4 sph = __ldg(sp);
+                const uint4 s1 = __ldg(reinterpret_cast<const uint4*>(sp + 1));  // materialId, lodOffset, lodCount, vertexOffset
+                if (s1.y < sc.lodCount && s1.z <= sc.lodCount - s1.y) {
+                    const Vec3 c = view_transform(v.rows, model_to_world(Vec3{sph.x, sph.y, sph.z}, ps[k], q[k]));
+                    const float r = BLZ_FM(sph.w, ps[k].w);
+                    inFrustum = frustum_check(c, r, v);
+                    cx[k] = c.x;
+                    cy[k] = c.y;
+                    cz[k] = c.z;
+                    cr[k] = r;
+                    lodOff[k] = s1.y;
+                    lodCnt[k] = s1.z;
+                } else {
+                    flags |= BLZ_FLAG_BAD_INDEX;
+                }
+            } else if (act[k]) {
                 flags |= BLZ_FLAG_BAD_INDEX;
             }
-        } else if (act[k]) {
-            flags |= BLZ_FLAG_BAD_INDEX;
+            if (MODE == BLZ_MODE_LATE && act[k] && !inFrustum) bv.vis[sb + k * 32u + lane] = 0u;  // drawOccLate.cs.hlsl:67
+            survivors[k] = __ballot_sync(0xFFFFFFFFu, inFrustum);
+            before[k + 1] = before[k] + __popc(survivors[k]);
         }
-        sm.visible[idx] = 0;
-        sm.result[idx] = kNotEmitted;
-        // append the survivors: one shared atomic per warp
-        const unsigned b = __ballot_sync(0xFFFFFFFFu, inFrustum);
-        uint32_t at = 0;
-        if (lane == 0 && b) at = atomicAdd(&sm.queueLen, static_cast<uint32_t>(__popc(b)));
-        at = __shfl_sync(0xFFFFFFFFu, at, 0) + __popc(b & lt);
-        if (inFrustum) {
-            const bool want = (MODE == BLZ_MODE_LATE) ? (visPrev[k] == 0u) : true;
-            sm.qx[at] = c.x;
-            sm.qy[at] = c.y;
-            sm.qz[at] = c.z;
-            sm.qr[at] = r;
-            sm.qs[at] = ps[k].w;
-            sm.qidx[at] = idx | (want ? 0x80000000u : 0u);
-            sm.qlodOff[at] = s1.y;
-            sm.qlodCnt[at] = s1.z;
-        }
-    }
-    __syncthreads();
-    // B: dense work over the survivors
-    const uint32_t n = sm.queueLen;
-    for (uint32_t j = threadIdx.x; j < n; j += THREADS) {
-        const Vec3 c{sm.qx[j], sm.qy[j], sm.qz[j]};
-        const float r = sm.qr[j];
-        const uint32_t id = sm.qidx[j];
-        bool visible = true;
-        if (MODE == BLZ_MODE_LATE || MODE == BLZ_MODE_TEMPORAL) {
-            float4 aabb;
-            if (project_sphere(c, r, v.zNear, v.proj0, v.proj5, aabb)) visible = occlusion(aabb, bv.pyr, v, c, r);
-        }
-        const uint32_t idx = id & 0x7FFFFFFFu;
-        sm.visible[idx] = visible ? 1 : 0;
-        if (visible && (id & 0x80000000u)) {
-            // cullBuffers.hlsl:42-55 — last LOD in [1, lodCount) with error < threshold
-            const uint32_t lodOff = sm.qlodOff[j], lodCnt = sm.qlodCnt[j];
-            const float threshold = lod_threshold(c, r, sm.qs[j], v.lodTarget);
-            uint32_t sel = 0;
-            for (uint32_t t = 1; t < lodCnt; ++t)
-                if (__ldg(&sc.lods[lodOff + t].error) < threshold) sel = t;
-            sm.result[idx] = lodOff + sel;
-        }
-    }
-    __syncthreads();
-    // C: results back to the owning threads, in object order
+        const uint32_t n = before[OPT];
+        // 2. dense rounds over the survivors, in object order
+        for (uint32_t jb = 0; jb < n; jb += 32u) {
+            const uint32_t j = jb + lane;
+            const bool mine = j < n;
+            int kk = 0;
 #pragma unroll
-    for (int k = 0; k < OPT; ++k) {
-        const uint32_t idx = k * THREADS + threadIdx.x;
-        const uint32_t res = sm.result[idx];
-        emit[k] = res != kNotEmitted;
-        lodId[k] = res;
-        if (MODE == BLZ_MODE_LATE && act[k]) bv.vis[base + idx] = sm.visible[idx];  // drawOccLate.cs.hlsl:67
+            for (int k = 1; k < OPT; ++k)
+                if (j >= before[k]) kk = k;
+            uint32_t src = lane;
+            if (mine) src = __fns(survivors[kk], 0u, static_cast<int>(j - before[kk]) + 1);
+            float fx = 0.f, fy = 0.f, fz = 0.f, fr = 0.f, fs = 0.f;
+            uint32_t fo = 0u, fc = 0u, fv = 0u;
+#pragma unroll
+            for (int k = 0; k < OPT; ++k) {  // every lane takes part in every shuffle
+                const float x = __shfl_sync(0xFFFFFFFFu, cx[k], src), y = __shfl_sync(0xFFFFFFFFu, cy[k], src);
+                const float z = __shfl_sync(0xFFFFFFFFu, cz[k], src), r = __shfl_sync(0xFFFFFFFFu, cr[k], src);
+                const float sc_ = __shfl_sync(0xFFFFFFFFu, ps[k].w, src);
+                const uint32_t o = __shfl_sync(0xFFFFFFFFu, lodOff[k], src), c = __shfl_sync(0xFFFFFFFFu, lodCnt[k], src);
+                const uint32_t vp = __shfl_sync(0xFFFFFFFFu, visPrev[k], src);
+                if (k == kk) {
+                    fx = x; fy = y; fz = z; fr = r; fs = sc_; fo = o; fc = c; fv = vp;
+                }
+            }
+            bool visible = mine;
+            uint32_t lid = 0u;
+            const uint32_t obj = sb + static_cast<uint32_t>(kk) * 32u + src;
+            if (mine) {
+                const Vec3 c{fx, fy, fz};
+                if (MODE == BLZ_MODE_LATE || MODE == BLZ_MODE_TEMPORAL) {
+                    float4 aabb;
+                    if (project_sphere(c, fr, v.zNear, v.proj0, v.proj5, aabb)) visible = occlusion(aabb, bv.pyr, v, c, fr);
+                }
+                if (MODE == BLZ_MODE_LATE) bv.vis[obj] = visible ? 1u : 0u;  // drawOccLate.cs.hlsl:67
+            }
+            bool emitted = visible && (MODE == BLZ_MODE_LATE ? fv == 0u : true);  // drawOccLate.cs.hlsl:45
+            if (emitted) {
+                // cullBuffers.hlsl:42-55 — last LOD in [1, lodCount) with error < threshold
+                const float threshold = lod_threshold(Vec3{fx, fy, fz}, fr, fs, v.lodTarget);
+                uint32_t sel = 0;
+                for (uint32_t t = 1; t < fc; ++t)
+                    if (__ldg(&sc.lods[fo + t].error) < threshold) sel = t;
+                lid = fo + sel;
+            }
+            // 3. stage the emitted ones in order
+            const unsigned e = __ballot_sync(0xFFFFFFFFu, emitted);
+            if (emitted) stage[run + __popc(e & lanemask_lt())] = make_uint2(obj, lid);
+            run += __popc(e);
+        }
     }
+    return run;
 }
 
 // Writes one record {objId, indexCount, 1, firstIndex, 0, 0}; pad words of 32-byte records are
@@ -204,51 +215,6 @@ __device__ __forceinline__ void put_record(uint8_t* cmds, uint32_t stride, uint3
         w[1] = make_uint2(1u, firstIndex);
         w[2] = make_uint2(0u, 0u);
     }
-}
-
-// Block-wide stable ranking of OPT ballots per thread in k-major order (object index order).
-// Returns the block's count (valid in warp 0); s_off[k * NW + w] becomes the exclusive offset of
-// (k, warp w) once the caller has synchronised.
-template <int THREADS, int OPT>
-__device__ __forceinline__ uint32_t block_rank(const bool (&emit)[OPT], uint32_t (&lrank)[OPT], uint32_t* s_off) {
-    constexpr int NW = THREADS / 32;
-    constexpr int M = OPT * NW;
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t lt = lanemask_lt();
-#pragma unroll
-    for (int k = 0; k < OPT; ++k) {
-        const unsigned b = __ballot_sync(0xFFFFFFFFu, emit[k]);
-        lrank[k] = __popc(b & lt);
-        if (lane == 0) s_off[k * NW + warp] = __popc(b);
-    }
-    __syncthreads();
-    uint32_t total = 0;
-    if (warp == 0) {
-        constexpr int E = (M + 31) / 32;
-        uint32_t vals[E];
-        uint32_t sum = 0;
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const int idx = lane * E + e;
-            vals[e] = idx < M ? s_off[idx] : 0u;
-            sum += vals[e];
-        }
-        uint32_t incl = sum;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= static_cast<uint32_t>(o)) incl += n;
-        }
-        uint32_t run = incl - sum;
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const int idx = lane * E + e;
-            if (idx < M) s_off[idx] = run;
-            run += vals[e];
-        }
-        total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    }
-    return total;
 }
 
 // Segmented exclusive scan of the chunk counts by one block, segments being the views: every
@@ -355,42 +321,32 @@ __device__ __forceinline__ void scan_chunk_counts(const PipeParams& p, uint32_t*
 template <int MODE, bool SINGLE, int THREADS, int OPT>
 __global__ void __launch_bounds__(THREADS) cull_decide_kernel(const PipeParams p) {
     constexpr int NW = THREADS / 32;
-    constexpr uint32_t CHUNK = THREADS * OPT;
-    __shared__ uint32_t s_off[OPT * NW];
     __shared__ uint32_t s_sum[NW], s_flag[NW];
     __shared__ int s_last;
-    __shared__ DecideSmem<CHUNK> s_dec;
-    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warpsTotal = gridDim.x * NW;
     unsigned int flags = 0u;
-    for (uint32_t chunk = blockIdx.x; chunk < p.totalTiles; chunk += gridDim.x) {
+    for (uint32_t chunk = blockIdx.x * NW + (threadIdx.x >> 5); chunk < p.totalTiles; chunk += warpsTotal) {
         uint32_t vi = 0, first = 0;
         if constexpr (!SINGLE) {
             vi = find_view(p.tileStart, p.viewCount, chunk);
             first = __ldg(p.tileStart + vi);
         }
         const BatchViewDev& bv = view_of<SINGLE>(p, vi);
-        const uint32_t base = (chunk - first) * CHUNK;
-        bool emit[OPT];
-        uint32_t lod[OPT];
+        const uint32_t base = (chunk - first) * kChunk;
+        uint2* stage = p.staged + static_cast<size_t>(chunk) * kChunk;
+        uint32_t total = 0;
         if (MODE == kModeRuntime) {
             switch (bv.mode) {
-                case BLZ_MODE_FIRST: decide_chunk<BLZ_MODE_FIRST, THREADS, OPT>(p.sc, bv, base, s_dec, emit, lod, flags); break;
-                case BLZ_MODE_LATE: decide_chunk<BLZ_MODE_LATE, THREADS, OPT>(p.sc, bv, base, s_dec, emit, lod, flags); break;
-                case BLZ_MODE_TEMPORAL: decide_chunk<BLZ_MODE_TEMPORAL, THREADS, OPT>(p.sc, bv, base, s_dec, emit, lod, flags); break;
-                default: decide_chunk<BLZ_MODE_FRUSTUM, THREADS, OPT>(p.sc, bv, base, s_dec, emit, lod, flags); break;
+                case BLZ_MODE_FIRST: total = decide_chunk_warp<BLZ_MODE_FIRST, OPT>(p.sc, bv, base, stage, flags); break;
+                case BLZ_MODE_LATE: total = decide_chunk_warp<BLZ_MODE_LATE, OPT>(p.sc, bv, base, stage, flags); break;
+                case BLZ_MODE_TEMPORAL: total = decide_chunk_warp<BLZ_MODE_TEMPORAL, OPT>(p.sc, bv, base, stage, flags); break;
+                default: total = decide_chunk_warp<BLZ_MODE_FRUSTUM, OPT>(p.sc, bv, base, stage, flags); break;
             }
         } else {
-            decide_chunk<(MODE < 0 ? 0 : MODE), THREADS, OPT>(p.sc, bv, base, s_dec, emit, lod, flags);
+            total = decide_chunk_warp<(MODE < 0 ? 0 : MODE), OPT>(p.sc, bv, base, stage, flags);
         }
-        uint32_t lrank[OPT];
-        const uint32_t total = block_rank<THREADS, OPT>(emit, lrank, s_off);
-        if (threadIdx.x == 0) p.chunkCount[chunk] = total;
-        __syncthreads();  // warp 0's offsets are visible to every warp
-        uint2* stage = p.staged + static_cast<size_t>(chunk) * CHUNK;
-#pragma unroll
-        for (int k = 0; k < OPT; ++k)
-            if (emit[k]) stage[s_off[k * NW + warp] + lrank[k]] = make_uint2(base + k * THREADS + threadIdx.x, lod[k]);
-        __syncthreads();  // s_off is rewritten by the next chunk
+        if (lane == 0) p.chunkCount[chunk] = total;
     }
     if (flags) atomicOr(&p.scratch->status, flags);
 
@@ -441,7 +397,8 @@ static cudaError_t launch_t(const PipeParams& p, uint32_t blocksPerSm, int smCou
     const uint32_t per = blocksPerSm ? (blocksPerSm < static_cast<uint32_t>(occ) ? blocksPerSm : static_cast<uint32_t>(occ))
                                      : static_cast<uint32_t>(occ);
     uint32_t grid = per * static_cast<uint32_t>(smCount);
-    if (grid > p.totalTiles) grid = p.totalTiles;
+    const uint32_t needed = (p.totalTiles + THREADS / 32 - 1) / (THREADS / 32);  // one warp per chunk at most
+    if (grid > needed) grid = needed;
     if (grid == 0) grid = 1;
     kern<<<grid, THREADS, 0, s>>>(p);
     e = cudaGetLastError();
@@ -450,11 +407,11 @@ static cudaError_t launch_t(const PipeParams& p, uint32_t blocksPerSm, int smCou
     const uint32_t maxGrid = 16u * static_cast<uint32_t>(smCount);
     if (sgrid > maxGrid) sgrid = maxGrid;
     if (sgrid == 0) sgrid = 1;
-    cull_scatter_kernel<SINGLE><<<sgrid, 256, 0, s>>>(p, THREADS * OPT);
+    cull_scatter_kernel<SINGLE><<<sgrid, 256, 0, s>>>(p, kChunk);
     return cudaGetLastError();
 }
 
-uint32_t object_tile_size() { return kObjThreads * kObjOpt; }
+uint32_t object_tile_size() { return kChunk; }
 
 bool single_shape_supported(uint32_t threads, uint32_t opt) {
     return (threads == 256 && (opt == 1 || opt == 2 || opt == 4)) || (threads == 128 && (opt == 2 || opt == 4)) ||

@@ -82,6 +82,27 @@ class DevicePyramid:
         return self.storage[off: off + w * h].cpu().numpy().reshape(h, w)
 
 
+class Graph:
+    """A recorded sequence of library calls (blz_capture_begin / blz_capture_end)."""
+
+    def __init__(self, lib, handle, kernels: int):
+        self.lib, self.handle, self.kernels = lib, handle, kernels
+
+    def launch(self, stream=None) -> None:
+        check(self.lib.blz_graph_launch(self.handle, _stream_ptr(stream)), "blz_graph_launch")
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.blz_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Culler:
     """One library context: resident scene tables, scratch and status word for one stream."""
 
@@ -196,6 +217,17 @@ class Culler:
         check(self.lib.blz_depth_raster_boxes(self.ctx, C.byref(view), boxes.data_ptr(), boxes.numel() // 6,
                                               depth.data_ptr(), width, height, _stream_ptr(stream)),
               "blz_depth_raster_boxes")
+
+    # ------------------------------------------------------------------ recorded frames
+
+    def capture_begin(self, stream=None) -> None:
+        """Starts recording this context's calls on `stream` (a non-default stream) into a graph."""
+        check(self.lib.blz_capture_begin(self.ctx, _stream_ptr(stream)), "blz_capture_begin")
+
+    def capture_end(self, stream=None) -> "Graph":
+        g, k = C.c_void_p(), C.c_uint32(0)
+        check(self.lib.blz_capture_end(self.ctx, _stream_ptr(stream), C.byref(g), C.byref(k)), "blz_capture_end")
+        return Graph(self.lib, g, int(k.value))
 
     # ------------------------------------------------------------------ launch shape
 

@@ -283,6 +283,22 @@ int blz_set_launch_shape(blz_ctx* ctx, const BlzLaunchShape* shape);
 int blz_autotune_batch(blz_ctx* ctx, const BlzBatchView* views, uint32_t viewCount, uint32_t repeats,
                        blz_stream_t stream, BlzLaunchShape* best, float* bestMicroseconds);
 
+/* ---------------------------------------------------------------- recorded frames */
+
+typedef struct blz_graph blz_graph;
+
+/* Records every library call enqueued on `stream` between begin and end into a CUDA graph (stream
+ * capture, thread-local mode) and instantiates it; blz_graph_launch replays the whole sequence with
+ * one launch. Buffers, views and counts are the ones of the recorded calls. A first, unrecorded
+ * run of the same calls sizes the library's scratch, so nothing is allocated while recording.
+ * The reference records the same passes into a command buffer once per frame
+ * (src/Renderer/BlitzenVulkan/vulkanDraw.cpp:822-1122). kernelsOut (may be NULL) receives the
+ * number of this library's kernels in the graph. */
+int blz_capture_begin(blz_ctx* ctx, blz_stream_t stream);
+int blz_capture_end(blz_ctx* ctx, blz_stream_t stream, blz_graph** outGraph, uint32_t* kernelsOut);
+int blz_graph_launch(blz_graph* graph, blz_stream_t stream);
+int blz_graph_destroy(blz_graph* graph);
+
 /* ---------------------------------------------------------------- serving loop */
 
 typedef struct BlzServeConfig {
