@@ -39,6 +39,7 @@ HIZ_D3D12 = 0
 HIZ_VULKAN = 1
 MODE_FRUSTUM, MODE_FIRST, MODE_LATE, MODE_TEMPORAL = 0, 1, 2, 3
 SCENE_COPY_FROM_HOST, SCENE_BORROW_DEVICE = 0, 1
+NOALLOC_MAX_OBJECTS = 1 << 20
 
 FLAG_COMMAND_OVERFLOW = 1
 FLAG_INSTANCE_OVERFLOW = 2
@@ -165,6 +166,7 @@ _PROTOS = {
     "blz_pyramid_build": (_I, [_P, C.POINTER(Pyramid), _P, _P]),
     "blz_depth_raster_boxes": (_I, [_P, C.POINTER(CameraViewData), _P, _U32, _P, _U32, _U32, _P]),
     "blz_cull_frustum": (_I, [_P, C.POINTER(CameraViewData), RenderList, C.POINTER(CullTarget), _P]),
+    "blz_cull_frustum_noalloc": (_I, [_P, C.POINTER(CameraViewData), RenderList, C.POINTER(CullTarget), _P]),
     "blz_cull_first": (_I, [_P, C.POINTER(CameraViewData), RenderList, _P, C.POINTER(CullTarget), _P]),
     "blz_cull_late": (_I, [_P, C.POINTER(CameraViewData), RenderList, _P, C.POINTER(Pyramid), C.POINTER(CullTarget), _P]),
     "blz_cull_temporal": (_I, [_P, C.POINTER(CameraViewData), RenderList, C.POINTER(Pyramid), C.POINTER(CullTarget), _P]),

@@ -30,6 +30,7 @@ SOURCES = [
     "scene_kernels.cu",
     "serve.cpp",
     "view.cpp",
+    "noalloc.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,0 +1,113 @@
+// noalloc.cu — blz_cull_frustum_noalloc: the frustum + LOD cull with its per-call staging held in
+// a fixed array of this library's own device memory, so the call allocates nothing.
+//
+// blz_cull_frustum stages each chunk's emitted (object, LOD) pairs, the chunk counts, the chunk
+// prefixes and a done-blocks counter in context memory that grows on demand, and growing it means
+// cudaFree + cudaMalloc. Some callers cannot take that: a frame loop that has reserved all of its
+// device memory up front (another pool owns the rest, so a cudaMalloc would fail mid-frame), or
+// one that must never stall, since cudaFree waits for the whole device. This entry point runs the
+// same two kernels with that staging in `g_noallocScratch` below, a file-scope array sized for at
+// most BLZ_NOALLOC_MAX_OBJECTS render objects, and rejects larger lists instead of growing.
+//
+// Set-up: the array's device address is fetched with cudaGetSymbolAddress once per device, by
+// the first call made with that device current, and the done-blocks counter is cleared there
+// with a blocking cudaMemset. That first call therefore has to come before any stream capture.
+// After set-up a call only validates its arguments and launches.
+//
+// Only the done-blocks counter must start at zero; the decide kernel's last block puts it back
+// to zero at the end of every call. Every other word is written before it is read in each call.
+//
+// The array is one per device for the whole process, shared by every context on that device:
+// two calls that overlap on the device (two streams, two threads, two contexts) race on it and
+// both results are undefined. Order such calls on one stream, or with events.
+#include <mutex>
+
+#include "api_internal.h"
+
+namespace {
+
+using namespace blz;
+
+constexpr uint32_t kNoAllocChunk = 512;  // objects per chunk; must equal object_tile_size()
+constexpr uint32_t kNoAllocChunks = BLZ_NOALLOC_MAX_OBJECTS / kNoAllocChunk;
+static_assert(BLZ_NOALLOC_MAX_OBJECTS % kNoAllocChunk == 0, "the object bound must be whole chunks");
+
+// layout: staged records | chunk counts | chunk prefixes | done-blocks counter (own 256-byte line)
+constexpr size_t kStagedBytes = size_t(BLZ_NOALLOC_MAX_OBJECTS) * sizeof(uint2);
+constexpr size_t kCountsOffset = kStagedBytes;
+constexpr size_t kPrefixOffset = kCountsOffset + size_t(kNoAllocChunks) * sizeof(uint32_t);
+constexpr size_t kDoneOffset = kPrefixOffset + size_t(kNoAllocChunks) * sizeof(uint32_t);
+constexpr size_t kNoAllocBytes = kDoneOffset + 256;
+static_assert(kPrefixOffset % 256 == 0 && kDoneOffset % 256 == 0, "regions start on 256-byte lines");
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setupLock;
+unsigned char* g_base[kMaxDevices] = {};  // device address of g_noallocScratch, per device
+
+// Fetches the array's address for `device` (which is current) on its first use.
+int scratch_base(int device, unsigned char** out) {
+    std::lock_guard<std::mutex> guard(g_setupLock);
+    if (!g_base[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress of the no-alloc scratch");
+        if (reinterpret_cast<uintptr_t>(p) % 256 != 0) return fail(BLZ_ERR_CUDA, "no-alloc scratch is not 256-byte aligned");
+        e = cudaMemset(static_cast<unsigned char*>(p) + kDoneOffset, 0, sizeof(unsigned int));
+        if (e != cudaSuccess) return cuda_fail(e, "clearing the no-alloc done counter");
+        g_base[device] = static_cast<unsigned char*>(p);
+    }
+    *out = g_base[device];
+    return BLZ_OK;
+}
+
+}  // namespace
+
+extern "C" int blz_cull_frustum_noalloc(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list,
+                                        const BlzCullTarget* target, blz_stream_t stream) {
+    if (!c || !view) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or view is NULL");
+    int rc = check_target(target);
+    if (rc != BLZ_OK) return rc;
+    const BlzRenderObject* objs = nullptr;
+    uint32_t count = 0;
+    rc = resolve_list(c, list, &objs, &count);
+    if (rc != BLZ_OK) return rc;
+    if (count > BLZ_NOALLOC_MAX_OBJECTS)
+        return fail(BLZ_ERR_CAPACITY, "blz_cull_frustum_noalloc takes at most %u render objects, got %u",
+                    BLZ_NOALLOC_MAX_OBJECTS, count);
+    if (object_tile_size() != kNoAllocChunk) return fail(BLZ_ERR_CUDA, "no-alloc chunk size does not match the kernels");
+    int device = -1;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (device != c->device) return fail(BLZ_ERR_INVALID_ARGUMENT, "device %d is current, the context is on device %d", device, c->device);
+    if (device < 0 || device >= kMaxDevices) return fail(BLZ_ERR_INVALID_ARGUMENT, "device %d out of range", device);
+    unsigned char* base = nullptr;
+    rc = scratch_base(device, &base);
+    if (rc != BLZ_OK) return rc;
+
+    uint32_t chunks = (count + kNoAllocChunk - 1) / kNoAllocChunk;
+    if (chunks == 0) chunks = 1;  // an empty list still gets one chunk, and its draw count is written
+    PipeParams p{};
+    p.sc = c->scene;
+    p.single.view = *view;
+    p.single.objects = objs;
+    p.single.count = count;
+    p.single.mode = BLZ_MODE_FRUSTUM;
+    p.single.cmds = static_cast<uint8_t*>(target->commands);
+    p.single.stride = target->stride;
+    p.single.capacity = target->capacity;
+    p.single.drawCount = target->drawCount;
+    p.viewCount = 1;
+    p.totalTiles = chunks;
+    p.scratch = c->scratch;  // status flags stay in the context, read by blz_ctx_check
+    p.staged = reinterpret_cast<uint2*>(base);
+    p.chunkCount = reinterpret_cast<uint32_t*>(base + kCountsOffset);
+    p.chunkPrefix = reinterpret_cast<uint32_t*>(base + kPrefixOffset);
+    p.doneBlocks = reinterpret_cast<unsigned int*>(base + kDoneOffset);
+    e = launch_object_cull(BLZ_MODE_FRUSTUM, p, c->singleThreads, c->singleOpt, c->smCount,
+                           reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "no-alloc cull launch");
+    c->launches += 2;  // decide + scatter
+    return BLZ_OK;
+}

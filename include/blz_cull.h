@@ -192,6 +192,18 @@ typedef struct BlzCullTarget {
 int blz_cull_frustum(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
                      const BlzCullTarget* target, blz_stream_t stream);
 
+/* blz_cull_frustum without any device allocation. It has no counterpart in the reference: it
+ * exists for callers that cannot allocate device memory once running (their memory is reserved
+ * up front, or they must not wait on the device-wide synchronisation of cudaFree). Its per-call
+ * staging is a fixed device array inside this library, for at most BLZ_NOALLOC_MAX_OBJECTS render
+ * objects (8 MiB); longer lists return BLZ_ERR_CAPACITY. Results equal blz_cull_frustum's.
+ * The first call with a device current fetches that array's address and clears its counter
+ * (a blocking cudaMemset), so make it before any stream capture. The array is shared by every
+ * context on the device: calls that overlap on the device race on it and must be ordered. */
+#define BLZ_NOALLOC_MAX_OBJECTS (1u << 20)
+int blz_cull_frustum_noalloc(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
+                             const BlzCullTarget* target, blz_stream_t stream);
+
 /* Occlusion pass 1: objects with visibility[i] != 0 are frustum-tested and, when visible, emitted.
  * visibility is a device uint32 per render object (read only here).
  * Replaces InitialDrawCull.comp.glsl:12-59 / drawOccFirst.cs.hlsl:13-58 and DrawCullFirstPass
