@@ -295,7 +295,7 @@ def main():
     t_first = sum(ms_first) / len(ms_first)
     t_pyr = sum(ms_pyr) / len(ms_pyr)
     ach = bytes_late / (t_late * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "cull_objects_kernel<LATE> (pass 2)", "achieved": ach, "peak": peak,
+    roofline = {"bound": "hbm", "kernel": "pass 2: cull_decide_kernel<LATE> + cull_scatter_kernel", "achieved": ach, "peak": peak,
                 "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind, "traffic": None,
                 "algorithmic_bytes": bytes_late, "ms": t_late,
                 "others": {

@@ -40,7 +40,13 @@ def lib() -> C.CDLL:
         _lib.bo_ftou.restype = U
         _lib.bo_floor_log2_u.argtypes = [C.c_float]
         _lib.bo_floor_log2_u.restype = U
+        _lib.bo_object_test.argtypes = [C.c_int, P, P, _RenderObject, P, C.POINTER(U)]
+        _lib.bo_object_test.restype = C.c_int
     return _lib
+
+
+class _RenderObject(C.Structure):
+    _fields_ = [("transformId", C.c_uint32), ("surfaceId", C.c_uint32)]
 
 
 def _ptr(a: np.ndarray | None):
@@ -171,3 +177,13 @@ def ftou(x: float) -> int:
 
 def floor_log2_u(x: float) -> int:
     return int(lib().bo_floor_log2_u(x))
+
+
+def object_test(mode: int, view: CameraViewData, scene, obj_index: int, pyramid: HostPyramid | None = None):
+    """One object's decision: (visible 0/1 or -1 on a bad index, chosen global LOD index or None)."""
+    d, keep = scene_desc(scene)
+    o = keep[0][obj_index]
+    lod = C.c_uint32(0xFFFFFFFF)
+    v = lib().bo_object_test(mode, C.byref(view), C.byref(d), _RenderObject(int(o["transformId"]), int(o["surfaceId"])),
+                             C.byref(pyramid.desc) if pyramid else None, C.byref(lod))
+    return int(v), (int(lod.value) if v > 0 else None)
