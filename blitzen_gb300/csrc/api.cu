@@ -430,7 +430,7 @@ static int object_cull(blz_ctx* c, uint32_t mode, const BlzCameraViewData* view,
         rc = check_pyramid(pyr, true);
         if (rc != BLZ_OK) return rc;
     }
-    const uint32_t tile = object_tile_size();
+    const uint32_t tile = single_chunk_size(mode, c->singleThreads, c->singleOpt, count, c->smCount);
     uint32_t tiles = (count + tile - 1) / tile;
     if (tiles == 0) tiles = 1;  // an empty list still gets one chunk, and its draw count is written
     rc = ensure_chunk_scratch(c, tiles, tile);
@@ -453,6 +453,7 @@ static int object_cull(blz_ctx* c, uint32_t mode, const BlzCameraViewData* view,
     p.tileStart = nullptr;
     p.viewCount = 1;
     p.totalTiles = tiles;
+    p.chunkSize = tile;
     bind_chunk_scratch(c, p);
     cudaError_t e = launch_object_cull(mode, p, c->singleThreads, c->singleOpt, c->smCount, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "cull launch");

@@ -84,6 +84,7 @@ static int upload_views(blz_ctx* c, const std::vector<BatchViewDev>& d, const st
     p.tileStart = reinterpret_cast<const uint32_t*>(static_cast<char*>(dst) + tsOff);
     p.viewCount = n;
     p.totalTiles = ts[n];
+    p.chunkSize = object_tile_size();
     p.scratch = c->scratch;
     return BLZ_OK;
 }
@@ -214,6 +215,7 @@ int blz_cull_batch_per_view(blz_ctx* c, const BlzBatchView* views, uint32_t n, b
         p.tileStart = nullptr;
         p.viewCount = 1;
         p.totalTiles = ts[i + 1] - ts[i];
+        p.chunkSize = object_tile_size();
         bind_chunk_scratch(c, p);
         cudaError_t e = launch_object_cull(d[i].mode, p, c->singleThreads, c->singleOpt, c->smCount, st);
         if (e != cudaSuccess) return cuda_fail(e, "per-view cull launch");

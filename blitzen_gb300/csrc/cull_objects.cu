@@ -48,30 +48,75 @@ __device__ __forceinline__ uint32_t find_view(const uint32_t* tileStart, uint32_
 
 // ------------------------------------------------------------------ decisions
 
-constexpr uint32_t kChunk = 512;  // objects per chunk: the unit of staging, counting and scanning
+constexpr uint32_t kChunk = 512;  // objects per chunk of batched views (single views size theirs)
 
-// One warp decides a chunk of kChunk consecutive render objects of a view, 32 * OPT at a time
-// (object base + k * 32 + lane for k < OPT, so the step is k-major and lanes ascend).
-// For each step:
-//   1  every lane loads its OPT render objects and then their transforms (all reads issued before
-//      any arithmetic) and runs the frustum test;
-//   2  the frustum survivors are ranked with ballots — survivor order is object order — and handed
-//      to dense lanes with __fns + shuffles, so the sphere projection, Hi-Z test (LATE/TEMPORAL)
-//      and LOD selection run on packed lanes, not on every lane of every warp with a survivor;
-//   3  the emitted survivors are ranked with one more ballot and appended to the chunk's staging
-//      as (objectId, lodId); LATE writes every object's new visibility.
-// No shared memory and no block barrier: warps never wait for one another.
+// A frustum survivor waiting for the dense stage (32 bytes, two 16-byte shared-memory words).
+struct Survivor {
+    uint32_t obj;      // object index within the view; bit 31: visible last frame (LATE)
+    float cx, cy, cz;  // view-space sphere centre
+    float r, scale;
+    uint32_t lodOff, lodCnt;
+};
+constexpr uint32_t kRing = 64;  // per-warp survivor ring: under 32 waiting plus one 32-object slice
+
+// Dense stage over n <= 32 queued survivors starting at ring index head, in object order: the sphere
+// projection and Hi-Z test (LATE/TEMPORAL), LATE's visibility write, LOD selection of the emitted
+// ones, and their staging as (objectId, lodId) after the `run` already staged for the chunk.
+template <int MODE>
+__device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchViewDev& bv, const ViewConsts& v,
+                                            const Survivor* ring, uint32_t head, uint32_t n, uint2* stage,
+                                            uint32_t& run) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool mine = lane < n;
+    uint4 a = make_uint4(0u, 0u, 0u, 0u), b = make_uint4(0u, 0u, 0u, 0u);
+    if (mine) {
+        const uint4* e = reinterpret_cast<const uint4*>(ring + ((head + lane) & (kRing - 1u)));
+        a = e[0];
+        b = e[1];
+    }
+    const uint32_t obj = a.x & 0x7FFFFFFFu;
+    const Vec3 c{__uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(a.w)};
+    const float r = __uint_as_float(b.x), scale = __uint_as_float(b.y);
+    bool visible = mine;
+    if (mine) {
+        if (MODE == BLZ_MODE_LATE || MODE == BLZ_MODE_TEMPORAL) {
+            float4 aabb;
+            if (project_sphere(c, r, v.zNear, v.proj0, v.proj5, aabb)) visible = occlusion(aabb, bv.pyr, v, c, r);
+        }
+        if (MODE == BLZ_MODE_LATE) bv.vis[obj] = visible ? 1u : 0u;  // drawOccLate.cs.hlsl:67
+    }
+    const bool emitted = visible && (MODE == BLZ_MODE_LATE ? (a.x >> 31) == 0u : true);  // drawOccLate.cs.hlsl:45
+    uint32_t lid = 0u;
+    if (emitted) {
+        // cullBuffers.hlsl:42-55 — last LOD in [1, lodCount) with error < threshold
+        const float threshold = lod_threshold(c, r, scale, v.lodTarget);
+        uint32_t sel = 0;
+        for (uint32_t t = 1; t < b.w; ++t)
+            if (__ldg(&sc.lods[b.z + t].error) < threshold) sel = t;
+        lid = b.z + sel;
+    }
+    const unsigned e = __ballot_sync(0xFFFFFFFFu, emitted);
+    if (emitted) stage[run + __popc(e & lanemask_lt())] = make_uint2(obj, lid);
+    run += __popc(e);
+}
+
+// One warp decides the objects [base, limit) of a view, 32 * OPT at a time (object
+// sb + k * 32 + lane for k < OPT, so lanes ascend within each 32-object slice):
+//   1  every lane loads its OPT render objects (fetched one step ahead) and their transforms and
+//      surfaces, and runs the frustum test;
+//   2  each slice's survivors are appended, in object order, to the warp's ring in shared memory;
+//      whenever 32 are waiting they go through the dense stage on full lanes, so the costly part
+//      (projection, Hi-Z, LOD) never runs on a lane without an object;
+//   3  the dense stage stages the emitted ones in order; the rest drains at the end.
+// Returns the number of records staged. No block barrier: warps never wait for one another.
 template <int MODE, int OPT>
-__device__ __forceinline__ uint32_t decide_chunk_warp(const SceneTables& sc, const BatchViewDev& bv, uint32_t base,
-                                                      uint2* stage, unsigned int& flags) {
+__device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const BatchViewDev& bv, uint32_t base,
+                                                    uint32_t limit, uint2* stage, Survivor* ring,
+                                                    unsigned int& flags) {
     constexpr uint32_t STEP = 32u * OPT;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t count = bv.count;
     const ViewConsts v = load_view(bv.view);
-    uint32_t run = 0;  // emitted so far in this chunk
-    const uint32_t limit = min(base + kChunk, count);
-    // render objects and visibility words of the next step are fetched one step ahead, so a step
-    // waits on one DRAM latency (its transforms), not two
+    uint32_t run = 0, head = 0, tail = 0;
     uint2 nro[OPT];
     uint32_t nvis[OPT];
     auto prefetch = [&](uint32_t at) {
@@ -85,118 +130,77 @@ __device__ __forceinline__ uint32_t decide_chunk_warp(const SceneTables& sc, con
             if (MODE == BLZ_MODE_LATE && in) nvis[k] = bv.vis[i];  // rewritten later by this warp: coherent load
         }
     };
-    prefetch(base);
+    if (base < limit) prefetch(base);
     for (uint32_t sb = base; sb < limit; sb += STEP) {
-        // 1. loads, then the frustum test on the owning lane
         uint32_t visPrev[OPT];
         bool act[OPT];
         uint2 ro[OPT];
 #pragma unroll
         for (int k = 0; k < OPT; ++k) {
-            const uint32_t i = sb + k * 32u + lane;
-            act[k] = i < limit;
+            act[k] = sb + k * 32u + lane < limit;
             visPrev[k] = nvis[k];
             if (MODE == BLZ_MODE_FIRST) act[k] = act[k] && visPrev[k] != 0u;  // drawOccFirst.cs.hlsl:22-25
             ro[k] = act[k] ? nro[k] : make_uint2(0u, 0u);
         }
-        float4 ps[OPT], q[OPT];
+        float4 ps[OPT], q[OPT], sph[OPT];
+        uint4 s1[OPT];
         bool ok[OPT];
 #pragma unroll
         for (int k = 0; k < OPT; ++k) {
             ok[k] = act[k] && ro[k].x < sc.transformCount && ro[k].y < sc.surfaceCount;
             ps[k] = make_float4(0.f, 0.f, 0.f, 1.f);
             q[k] = make_float4(0.f, 0.f, 0.f, 1.f);
+            sph[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            s1[k] = make_uint4(0u, 0u, 0u, 0u);
             if (ok[k]) {
                 const BlzMeshTransform* t = ((bv.dynT != nullptr && ro[k].x < bv.dynCount) ? bv.dynT : sc.transforms) + ro[k].x;
                 const float4* tp = reinterpret_cast<const float4*>(t);
                 ps[k] = __ldg(tp);
                 q[k] = __ldg(tp + 1);
+                const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + ro[k].y);
+                sph[k] = __ldg(sp);
+                s1[k] = __ldg(reinterpret_cast<const uint4*>(sp + 1));  // materialId, lodOffset, lodCount, vertexOffset
             }
         }
         if (sb + STEP < limit) prefetch(sb + STEP);
-        float cx[OPT], cy[OPT], cz[OPT], cr[OPT];
-        uint32_t lodOff[OPT], lodCnt[OPT];
-        unsigned survivors[OPT];
-        uint32_t before[OPT + 1];
-        before[0] = 0;
 #pragma unroll
         for (int k = 0; k < OPT; ++k) {
             bool inFrustum = false;
-            cx[k] = cy[k] = cz[k] = cr[k] = 0.f;
-            lodOff[k] = lodCnt[k] = 0u;
+            Vec3 c{0.f, 0.f, 0.f};
+            float r = 0.f;
             if (ok[k]) {
-                const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + ro[k].y);
-                const float4 sph = __ldg(sp);
-                const uint4 s1 = __ldg(reinterpret_cast<const uint4*>(sp + 1));  // materialId, lodOffset, lodCount, vertexOffset
-                if (s1.y < sc.lodCount && s1.z <= sc.lodCount - s1.y) {
-                    const Vec3 c = view_transform(v.rows, model_to_world(Vec3{sph.x, sph.y, sph.z}, ps[k], q[k]));
-                    const float r = BLZ_FM(sph.w, ps[k].w);
+                if (s1[k].y < sc.lodCount && s1[k].z <= sc.lodCount - s1[k].y) {
+                    c = view_transform(v.rows, model_to_world(Vec3{sph[k].x, sph[k].y, sph[k].z}, ps[k], q[k]));
+                    r = BLZ_FM(sph[k].w, ps[k].w);
                     inFrustum = frustum_check(c, r, v);
-                    cx[k] = c.x;
-                    cy[k] = c.y;
-                    cz[k] = c.z;
-                    cr[k] = r;
-                    lodOff[k] = s1.y;
-                    lodCnt[k] = s1.z;
                 } else {
                     flags |= BLZ_FLAG_BAD_INDEX;
                 }
             } else if (act[k]) {
                 flags |= BLZ_FLAG_BAD_INDEX;
             }
-            if (MODE == BLZ_MODE_LATE && act[k] && !inFrustum) bv.vis[sb + k * 32u + lane] = 0u;  // drawOccLate.cs.hlsl:67
-            survivors[k] = __ballot_sync(0xFFFFFFFFu, inFrustum);
-            before[k + 1] = before[k] + __popc(survivors[k]);
+            const uint32_t i = sb + k * 32u + lane;
+            if (MODE == BLZ_MODE_LATE && act[k] && !inFrustum) bv.vis[i] = 0u;  // drawOccLate.cs.hlsl:67
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, inFrustum);
+            if (inFrustum) {
+                uint4* e = reinterpret_cast<uint4*>(ring + ((tail + __popc(m & lanemask_lt())) & (kRing - 1u)));
+                const uint32_t tag = (MODE == BLZ_MODE_LATE && visPrev[k] != 0u) ? 0x80000000u : 0u;
+                e[0] = make_uint4(i | tag, __float_as_uint(c.x), __float_as_uint(c.y), __float_as_uint(c.z));
+                e[1] = make_uint4(__float_as_uint(r), __float_as_uint(ps[k].w), s1[k].y, s1[k].z);
+            }
+            tail += __popc(m);
+            if (tail - head >= 32u) {
+                __syncwarp();
+                dense_round<MODE>(sc, bv, v, ring, head, 32u, stage, run);
+                head += 32u;
+                __syncwarp();
+            }
         }
-        const uint32_t n = before[OPT];
-        // 2. dense rounds over the survivors, in object order
-        for (uint32_t jb = 0; jb < n; jb += 32u) {
-            const uint32_t j = jb + lane;
-            const bool mine = j < n;
-            int kk = 0;
-#pragma unroll
-            for (int k = 1; k < OPT; ++k)
-                if (j >= before[k]) kk = k;
-            uint32_t src = lane;
-            if (mine) src = __fns(survivors[kk], 0u, static_cast<int>(j - before[kk]) + 1);
-            float fx = 0.f, fy = 0.f, fz = 0.f, fr = 0.f, fs = 0.f;
-            uint32_t fo = 0u, fc = 0u, fv = 0u;
-#pragma unroll
-            for (int k = 0; k < OPT; ++k) {  // every lane takes part in every shuffle
-                const float x = __shfl_sync(0xFFFFFFFFu, cx[k], src), y = __shfl_sync(0xFFFFFFFFu, cy[k], src);
-                const float z = __shfl_sync(0xFFFFFFFFu, cz[k], src), r = __shfl_sync(0xFFFFFFFFu, cr[k], src);
-                const float sc_ = __shfl_sync(0xFFFFFFFFu, ps[k].w, src);
-                const uint32_t o = __shfl_sync(0xFFFFFFFFu, lodOff[k], src), c = __shfl_sync(0xFFFFFFFFu, lodCnt[k], src);
-                const uint32_t vp = __shfl_sync(0xFFFFFFFFu, visPrev[k], src);
-                if (k == kk) {
-                    fx = x; fy = y; fz = z; fr = r; fs = sc_; fo = o; fc = c; fv = vp;
-                }
-            }
-            bool visible = mine;
-            uint32_t lid = 0u;
-            const uint32_t obj = sb + static_cast<uint32_t>(kk) * 32u + src;
-            if (mine) {
-                const Vec3 c{fx, fy, fz};
-                if (MODE == BLZ_MODE_LATE || MODE == BLZ_MODE_TEMPORAL) {
-                    float4 aabb;
-                    if (project_sphere(c, fr, v.zNear, v.proj0, v.proj5, aabb)) visible = occlusion(aabb, bv.pyr, v, c, fr);
-                }
-                if (MODE == BLZ_MODE_LATE) bv.vis[obj] = visible ? 1u : 0u;  // drawOccLate.cs.hlsl:67
-            }
-            bool emitted = visible && (MODE == BLZ_MODE_LATE ? fv == 0u : true);  // drawOccLate.cs.hlsl:45
-            if (emitted) {
-                // cullBuffers.hlsl:42-55 — last LOD in [1, lodCount) with error < threshold
-                const float threshold = lod_threshold(Vec3{fx, fy, fz}, fr, fs, v.lodTarget);
-                uint32_t sel = 0;
-                for (uint32_t t = 1; t < fc; ++t)
-                    if (__ldg(&sc.lods[fo + t].error) < threshold) sel = t;
-                lid = fo + sel;
-            }
-            // 3. stage the emitted ones in order
-            const unsigned e = __ballot_sync(0xFFFFFFFFu, emitted);
-            if (emitted) stage[run + __popc(e & lanemask_lt())] = make_uint2(obj, lid);
-            run += __popc(e);
-        }
+    }
+    if (tail != head) {
+        __syncwarp();
+        dense_round<MODE>(sc, bv, v, ring, head, tail - head, stage, run);
+        __syncwarp();
     }
     return run;
 }
@@ -323,28 +327,32 @@ __global__ void __launch_bounds__(THREADS) cull_decide_kernel(const PipeParams p
     constexpr int NW = THREADS / 32;
     __shared__ uint32_t s_sum[NW], s_flag[NW];
     __shared__ int s_last;
-    const uint32_t lane = threadIdx.x & 31u;
+    __shared__ __align__(16) Survivor s_ring[NW][kRing];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t warpsTotal = gridDim.x * NW;
+    const uint32_t chunkSize = p.chunkSize;
     unsigned int flags = 0u;
-    for (uint32_t chunk = blockIdx.x * NW + (threadIdx.x >> 5); chunk < p.totalTiles; chunk += warpsTotal) {
+    for (uint32_t chunk = blockIdx.x * NW + warp; chunk < p.totalTiles; chunk += warpsTotal) {
         uint32_t vi = 0, first = 0;
         if constexpr (!SINGLE) {
             vi = find_view(p.tileStart, p.viewCount, chunk);
             first = __ldg(p.tileStart + vi);
         }
         const BatchViewDev& bv = view_of<SINGLE>(p, vi);
-        const uint32_t base = (chunk - first) * kChunk;
-        uint2* stage = p.staged + static_cast<size_t>(chunk) * kChunk;
+        const uint32_t base = (chunk - first) * chunkSize;
+        const uint32_t limit = min(base + chunkSize, bv.count);
+        uint2* stage = p.staged + static_cast<size_t>(chunk) * chunkSize;
+        Survivor* ring = s_ring[warp];
         uint32_t total = 0;
         if (MODE == kModeRuntime) {
             switch (bv.mode) {
-                case BLZ_MODE_FIRST: total = decide_chunk_warp<BLZ_MODE_FIRST, OPT>(p.sc, bv, base, stage, flags); break;
-                case BLZ_MODE_LATE: total = decide_chunk_warp<BLZ_MODE_LATE, OPT>(p.sc, bv, base, stage, flags); break;
-                case BLZ_MODE_TEMPORAL: total = decide_chunk_warp<BLZ_MODE_TEMPORAL, OPT>(p.sc, bv, base, stage, flags); break;
-                default: total = decide_chunk_warp<BLZ_MODE_FRUSTUM, OPT>(p.sc, bv, base, stage, flags); break;
+                case BLZ_MODE_FIRST: total = decide_run_warp<BLZ_MODE_FIRST, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
+                case BLZ_MODE_LATE: total = decide_run_warp<BLZ_MODE_LATE, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
+                case BLZ_MODE_TEMPORAL: total = decide_run_warp<BLZ_MODE_TEMPORAL, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
+                default: total = decide_run_warp<BLZ_MODE_FRUSTUM, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
             }
         } else {
-            total = decide_chunk_warp<(MODE < 0 ? 0 : MODE), OPT>(p.sc, bv, base, stage, flags);
+            total = decide_run_warp<(MODE < 0 ? 0 : MODE), OPT>(p.sc, bv, base, limit, stage, ring, flags);
         }
         if (lane == 0) p.chunkCount[chunk] = total;
     }
@@ -365,7 +373,8 @@ __global__ void __launch_bounds__(THREADS) cull_decide_kernel(const PipeParams p
 
 // Each warp copies one chunk's staged records to their final slots as full records.
 template <bool SINGLE>
-__global__ void __launch_bounds__(256) cull_scatter_kernel(const PipeParams p, uint32_t chunkSize) {
+__global__ void __launch_bounds__(256) cull_scatter_kernel(const PipeParams p) {
+    const uint32_t chunkSize = p.chunkSize;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warpsTotal = gridDim.x * (blockDim.x >> 5);
     for (uint32_t chunk = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); chunk < p.totalTiles; chunk += warpsTotal) {
@@ -387,31 +396,71 @@ __global__ void __launch_bounds__(256) cull_scatter_kernel(const PipeParams p, u
 
 // ------------------------------------------------------------------ launchers
 
+// Resident blocks per SM of one instantiation (a property of the kernel, asked once).
+template <int MODE, bool SINGLE, int THREADS, int OPT>
+static uint32_t occupancy_t() {
+    static const uint32_t occ = [] {
+        int o = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, cull_decide_kernel<MODE, SINGLE, THREADS, OPT>, THREADS, 0) !=
+            cudaSuccess) {
+            (void)cudaGetLastError();
+            o = 1;
+        }
+        return static_cast<uint32_t>(o < 1 ? 1 : o);
+    }();
+    return occ;
+}
+
 template <int MODE, bool SINGLE, int THREADS, int OPT>
 static cudaError_t launch_t(const PipeParams& p, uint32_t blocksPerSm, int smCount, cudaStream_t s) {
     auto kern = cull_decide_kernel<MODE, SINGLE, THREADS, OPT>;
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, THREADS, 0);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) occ = 1;
-    const uint32_t per = blocksPerSm ? (blocksPerSm < static_cast<uint32_t>(occ) ? blocksPerSm : static_cast<uint32_t>(occ))
-                                     : static_cast<uint32_t>(occ);
+    const uint32_t occ = occupancy_t<MODE, SINGLE, THREADS, OPT>();
+    const uint32_t per = blocksPerSm ? (blocksPerSm < occ ? blocksPerSm : occ) : occ;
     uint32_t grid = per * static_cast<uint32_t>(smCount);
     const uint32_t needed = (p.totalTiles + THREADS / 32 - 1) / (THREADS / 32);  // one warp per chunk at most
     if (grid > needed) grid = needed;
     if (grid == 0) grid = 1;
     kern<<<grid, THREADS, 0, s>>>(p);
-    e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     uint32_t sgrid = (p.totalTiles + 7) / 8;  // one warp per chunk
     const uint32_t maxGrid = 16u * static_cast<uint32_t>(smCount);
     if (sgrid > maxGrid) sgrid = maxGrid;
     if (sgrid == 0) sgrid = 1;
-    cull_scatter_kernel<SINGLE><<<sgrid, 256, 0, s>>>(p, kChunk);
+    cull_scatter_kernel<SINGLE><<<sgrid, 256, 0, s>>>(p);
     return cudaGetLastError();
 }
 
 uint32_t object_tile_size() { return kChunk; }
+
+template <int MODE>
+static uint32_t single_blocks_per_sm(uint32_t threads, uint32_t opt) {
+    if (threads == 256 && opt == 1) return occupancy_t<MODE, true, 256, 1>();
+    if (threads == 256 && opt == 4) return occupancy_t<MODE, true, 256, 4>();
+    if (threads == 128 && opt == 2) return occupancy_t<MODE, true, 128, 2>();
+    if (threads == 128 && opt == 4) return occupancy_t<MODE, true, 128, 4>();
+    if (threads == 512 && opt == 1) return occupancy_t<MODE, true, 512, 1>();
+    return occupancy_t<MODE, true, kObjThreads, kObjOpt>();
+}
+
+uint32_t single_chunk_size(uint32_t mode, uint32_t threads, uint32_t opt, uint32_t count, int smCount) {
+    if (!single_shape_supported(threads, opt)) {
+        threads = kObjThreads;
+        opt = kObjOpt;
+    }
+    uint32_t per = 1;
+    switch (mode) {
+        case BLZ_MODE_FIRST: per = single_blocks_per_sm<BLZ_MODE_FIRST>(threads, opt); break;
+        case BLZ_MODE_LATE: per = single_blocks_per_sm<BLZ_MODE_LATE>(threads, opt); break;
+        case BLZ_MODE_TEMPORAL: per = single_blocks_per_sm<BLZ_MODE_TEMPORAL>(threads, opt); break;
+        default: per = single_blocks_per_sm<BLZ_MODE_FRUSTUM>(threads, opt); break;
+    }
+    const uint64_t warps = static_cast<uint64_t>(per) * static_cast<uint64_t>(smCount > 0 ? smCount : 1) * (threads / 32u);
+    const uint32_t step = 32u * opt;
+    uint64_t size = (count + warps - 1) / warps;
+    size = (size + step - 1) / step * step;
+    return static_cast<uint32_t>(size < step ? step : size);
+}
 
 bool single_shape_supported(uint32_t threads, uint32_t opt) {
     return (threads == 256 && (opt == 1 || opt == 2 || opt == 4)) || (threads == 128 && (opt == 2 || opt == 4)) ||

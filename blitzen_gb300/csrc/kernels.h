@@ -81,6 +81,8 @@ struct PipeParams {
     const uint32_t* tileStart;
     uint32_t viewCount;
     uint32_t totalTiles;   // chunks over all views
+    uint32_t chunkSize;    // objects per chunk, a multiple of 32
+    uint32_t pad0;
     Scratch* scratch;      // status word
     uint2* staged;         // [totalTiles * chunkSize] (objectId, lodId)
     uint32_t* chunkCount;  // [totalTiles]
@@ -129,6 +131,9 @@ struct PyramidBuildParams {
 };
 
 uint32_t object_tile_size();
+// Chunk size of a single-view launch of `count` objects: one chunk per warp the launch holds
+// resident, so every warp streams one contiguous run of objects and none waits for a second round.
+uint32_t single_chunk_size(uint32_t mode, uint32_t threads, uint32_t opt, uint32_t count, int smCount);
 bool single_shape_supported(uint32_t threads, uint32_t opt);
 cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t threads, uint32_t opt, int smCount,
                                cudaStream_t s);

@@ -28,7 +28,7 @@ namespace {
 
 using namespace blz;
 
-constexpr uint32_t kNoAllocChunk = 512;  // objects per chunk; must equal object_tile_size()
+constexpr uint32_t kNoAllocChunk = 512;  // objects per chunk (the kernels take any multiple of 32)
 constexpr uint32_t kNoAllocChunks = BLZ_NOALLOC_MAX_OBJECTS / kNoAllocChunk;
 static_assert(BLZ_NOALLOC_MAX_OBJECTS % kNoAllocChunk == 0, "the object bound must be whole chunks");
 
@@ -76,7 +76,6 @@ extern "C" int blz_cull_frustum_noalloc(blz_ctx* c, const BlzCameraViewData* vie
     if (count > BLZ_NOALLOC_MAX_OBJECTS)
         return fail(BLZ_ERR_CAPACITY, "blz_cull_frustum_noalloc takes at most %u render objects, got %u",
                     BLZ_NOALLOC_MAX_OBJECTS, count);
-    if (object_tile_size() != kNoAllocChunk) return fail(BLZ_ERR_CUDA, "no-alloc chunk size does not match the kernels");
     int device = -1;
     cudaError_t e = cudaGetDevice(&device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
@@ -100,6 +99,7 @@ extern "C" int blz_cull_frustum_noalloc(blz_ctx* c, const BlzCameraViewData* vie
     p.single.drawCount = target->drawCount;
     p.viewCount = 1;
     p.totalTiles = chunks;
+    p.chunkSize = kNoAllocChunk;
     p.scratch = c->scratch;  // status flags stay in the context, read by blz_ctx_check
     p.staged = reinterpret_cast<uint2*>(base);
     p.chunkCount = reinterpret_cast<uint32_t*>(base + kCountsOffset);
