@@ -91,12 +91,13 @@ struct ViewRows {
     float4 r0, r1, r2;
 };
 
-// view * vec4(p, 1), terms summed left to right.
+// view * vec4(p, 1), terms summed left to right. The last term, m[12+k] * 1, is m[12+k] itself
+// (multiplying by one is exact; a NaN stays a NaN), so it is added without the multiply.
 __device__ __forceinline__ Vec3 view_transform(const ViewRows& m, Vec3 p) {
     Vec3 o;
-    o.x = BLZ_FA(BLZ_FA(BLZ_FA(BLZ_FM(m.r0.x, p.x), BLZ_FM(m.r0.y, p.y)), BLZ_FM(m.r0.z, p.z)), BLZ_FM(m.r0.w, 1.0f));
-    o.y = BLZ_FA(BLZ_FA(BLZ_FA(BLZ_FM(m.r1.x, p.x), BLZ_FM(m.r1.y, p.y)), BLZ_FM(m.r1.z, p.z)), BLZ_FM(m.r1.w, 1.0f));
-    o.z = BLZ_FA(BLZ_FA(BLZ_FA(BLZ_FM(m.r2.x, p.x), BLZ_FM(m.r2.y, p.y)), BLZ_FM(m.r2.z, p.z)), BLZ_FM(m.r2.w, 1.0f));
+    o.x = BLZ_FA(BLZ_FA(BLZ_FA(BLZ_FM(m.r0.x, p.x), BLZ_FM(m.r0.y, p.y)), BLZ_FM(m.r0.z, p.z)), m.r0.w);
+    o.y = BLZ_FA(BLZ_FA(BLZ_FA(BLZ_FM(m.r1.x, p.x), BLZ_FM(m.r1.y, p.y)), BLZ_FM(m.r1.z, p.z)), m.r1.w);
+    o.z = BLZ_FA(BLZ_FA(BLZ_FA(BLZ_FM(m.r2.x, p.x), BLZ_FM(m.r2.y, p.y)), BLZ_FM(m.r2.z, p.z)), m.r2.w);
     return o;
 }
 

@@ -103,18 +103,28 @@ __device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchVi
 // One warp decides the objects [base, limit) of a view, 32 * OPT at a time (object
 // sb + k * 32 + lane for k < OPT, so lanes ascend within each 32-object slice):
 //   1  every lane loads its OPT render objects (fetched one step ahead) and their transforms and
-//      surfaces, and runs the frustum test;
+//      surfaces, and runs the frustum test — without branches: an object that is out of range,
+//      not active in this pass or has a bad id reads the tables' first rows and is masked out;
 //   2  each slice's survivors are appended, in object order, to the warp's ring in shared memory;
 //      whenever 32 are waiting they go through the dense stage on full lanes, so the costly part
 //      (projection, Hi-Z, LOD) never runs on a lane without an object;
 //   3  the dense stage stages the emitted ones in order; the rest drains at the end.
 // Returns the number of records staged. No block barrier: warps never wait for one another.
-template <int MODE, int OPT>
+template <int MODE, bool SINGLE, int OPT>
 __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const BatchViewDev& bv, uint32_t base,
                                                     uint32_t limit, uint2* stage, Survivor* ring,
                                                     unsigned int& flags) {
     constexpr uint32_t STEP = 32u * OPT;
     const uint32_t lane = threadIdx.x & 31u;
+    if (sc.transformCount == 0u || sc.surfaceCount == 0u) {
+        // nothing can be looked up: every object of the pass has a bad id and none is visible
+        for (uint32_t i = base + lane; i < limit; i += 32u) {
+            const bool act = MODE != BLZ_MODE_FIRST || __ldg(bv.vis + i) != 0u;
+            if (act) flags |= BLZ_FLAG_BAD_INDEX;
+            if (MODE == BLZ_MODE_LATE) bv.vis[i] = 0u;
+        }
+        return 0u;
+    }
     const ViewConsts v = load_view(bv.view);
     uint32_t run = 0, head = 0, tail = 0;
     uint2 nro[OPT];
@@ -125,68 +135,54 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
             const uint32_t i = at + k * 32u + lane;
             const bool in = i < limit;
             nro[k] = in ? __ldg(reinterpret_cast<const uint2*>(bv.objects) + i) : make_uint2(0u, 0u);
-            nvis[k] = 1u;
+            nvis[k] = in ? 1u : 0u;
             if (MODE == BLZ_MODE_FIRST && in) nvis[k] = __ldg(bv.vis + i);
-            if (MODE == BLZ_MODE_LATE && in) nvis[k] = bv.vis[i];  // rewritten later by this warp: coherent load
+            if (MODE == BLZ_MODE_LATE && in) nvis[k] = bv.vis[i] | 0x80000000u;  // rewritten later by this warp: coherent load
         }
     };
     if (base < limit) prefetch(base);
     for (uint32_t sb = base; sb < limit; sb += STEP) {
         uint32_t visPrev[OPT];
-        bool act[OPT];
-        uint2 ro[OPT];
-#pragma unroll
-        for (int k = 0; k < OPT; ++k) {
-            act[k] = sb + k * 32u + lane < limit;
-            visPrev[k] = nvis[k];
-            if (MODE == BLZ_MODE_FIRST) act[k] = act[k] && visPrev[k] != 0u;  // drawOccFirst.cs.hlsl:22-25
-            ro[k] = act[k] ? nro[k] : make_uint2(0u, 0u);
-        }
+        bool act[OPT], ok[OPT];
         float4 ps[OPT], q[OPT], sph[OPT];
-        uint4 s1[OPT];
-        bool ok[OPT];
+        uint2 lod[OPT];
 #pragma unroll
         for (int k = 0; k < OPT; ++k) {
-            ok[k] = act[k] && ro[k].x < sc.transformCount && ro[k].y < sc.surfaceCount;
-            ps[k] = make_float4(0.f, 0.f, 0.f, 1.f);
-            q[k] = make_float4(0.f, 0.f, 0.f, 1.f);
-            sph[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-            s1[k] = make_uint4(0u, 0u, 0u, 0u);
-            if (ok[k]) {
-                const BlzMeshTransform* t = ((bv.dynT != nullptr && ro[k].x < bv.dynCount) ? bv.dynT : sc.transforms) + ro[k].x;
-                const float4* tp = reinterpret_cast<const float4*>(t);
-                ps[k] = __ldg(tp);
-                q[k] = __ldg(tp + 1);
-                const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + ro[k].y);
-                sph[k] = __ldg(sp);
-                s1[k] = __ldg(reinterpret_cast<const uint4*>(sp + 1));  // materialId, lodOffset, lodCount, vertexOffset
+            visPrev[k] = nvis[k];
+            // in range (LATE marks it in bit 31), and pass 1: visible last frame (drawOccFirst.cs.hlsl:22-25)
+            act[k] = visPrev[k] != 0u;
+            const uint2 ro = nro[k];
+            ok[k] = act[k] && ro.x < sc.transformCount && ro.y < sc.surfaceCount;
+            const uint32_t tid = ok[k] ? ro.x : 0u, sid = ok[k] ? ro.y : 0u;
+            const BlzMeshTransform* tt = sc.transforms;
+            if constexpr (!SINGLE) {
+                if (bv.dynT != nullptr && tid < bv.dynCount) tt = bv.dynT;
             }
+            const float4* tp = reinterpret_cast<const float4*>(tt + tid);
+            const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + sid);
+            ps[k] = __ldg(tp);
+            q[k] = __ldg(tp + 1);
+            sph[k] = __ldg(sp);
+            const uint4 s1 = __ldg(reinterpret_cast<const uint4*>(sp + 1));  // materialId, lodOffset, lodCount, vertexOffset
+            lod[k] = make_uint2(s1.y, s1.z);
         }
         if (sb + STEP < limit) prefetch(sb + STEP);
 #pragma unroll
         for (int k = 0; k < OPT; ++k) {
-            bool inFrustum = false;
-            Vec3 c{0.f, 0.f, 0.f};
-            float r = 0.f;
-            if (ok[k]) {
-                if (s1[k].y < sc.lodCount && s1[k].z <= sc.lodCount - s1[k].y) {
-                    c = view_transform(v.rows, model_to_world(Vec3{sph[k].x, sph[k].y, sph[k].z}, ps[k], q[k]));
-                    r = BLZ_FM(sph[k].w, ps[k].w);
-                    inFrustum = frustum_check(c, r, v);
-                } else {
-                    flags |= BLZ_FLAG_BAD_INDEX;
-                }
-            } else if (act[k]) {
-                flags |= BLZ_FLAG_BAD_INDEX;
-            }
+            const bool lodOk = lod[k].x < sc.lodCount && lod[k].y <= sc.lodCount - lod[k].x;
+            const bool good = ok[k] && lodOk;
+            if (act[k] && !good) flags |= BLZ_FLAG_BAD_INDEX;
+            const Vec3 c = view_transform(v.rows, model_to_world(Vec3{sph[k].x, sph[k].y, sph[k].z}, ps[k], q[k]));
+            const float r = BLZ_FM(sph[k].w, ps[k].w);
+            const bool inFrustum = good && frustum_check(c, r, v);
             const uint32_t i = sb + k * 32u + lane;
             if (MODE == BLZ_MODE_LATE && act[k] && !inFrustum) bv.vis[i] = 0u;  // drawOccLate.cs.hlsl:67
             const unsigned m = __ballot_sync(0xFFFFFFFFu, inFrustum);
             if (inFrustum) {
                 uint4* e = reinterpret_cast<uint4*>(ring + ((tail + __popc(m & lanemask_lt())) & (kRing - 1u)));
-                const uint32_t tag = (MODE == BLZ_MODE_LATE && visPrev[k] != 0u) ? 0x80000000u : 0u;
+                const uint32_t tag = (MODE == BLZ_MODE_LATE && (visPrev[k] & 0x7FFFFFFFu) != 0u) ? 0x80000000u : 0u;
                 e[0] = make_uint4(i | tag, __float_as_uint(c.x), __float_as_uint(c.y), __float_as_uint(c.z));
-                e[1] = make_uint4(__float_as_uint(r), __float_as_uint(ps[k].w), s1[k].y, s1[k].z);
+                e[1] = make_uint4(__float_as_uint(r), __float_as_uint(ps[k].w), lod[k].x, lod[k].y);
             }
             tail += __popc(m);
             if (tail - head >= 32u) {
@@ -294,27 +290,35 @@ __device__ __forceinline__ void scan_chunk_counts(const PipeParams& p, uint32_t*
         prevFlag = 0;
     }
     uint32_t carry = prevFlag ? prevSum : wsum + prevSum;
-    // pass 2: offsets, and each view's total at its last chunk
+    // pass 2: offsets, and each view's total at its last chunk (counts fetched eight at a time, so a
+    // run costs one L2 latency per eight chunks here too)
     {
         uint32_t v = vi, ns = nextStart, run = carry;
-        for (uint32_t c = r0; c < r1; ++c) {
-            if constexpr (!SINGLE) {
-                while (c >= ns) {
-                    ++v;
-                    ns = __ldg(p.tileStart + v + 1);
+        for (uint32_t c0 = r0; c0 < r1; c0 += 8) {
+            uint32_t x[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) x[u] = (c0 + u < r1) ? __ldcg(p.chunkCount + c0 + u) : 0u;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t c = c0 + u;
+                if (c >= r1) break;
+                if constexpr (!SINGLE) {
+                    while (c >= ns) {
+                        ++v;
+                        ns = __ldg(p.tileStart + v + 1);
+                    }
+                    if (c == __ldg(p.tileStart + v)) run = 0;
+                } else if (c == 0) {
+                    run = 0;
                 }
-                if (c == __ldg(p.tileStart + v)) run = 0;
-            } else if (c == 0) {
-                run = 0;
-            }
-            const uint32_t x = __ldcg(p.chunkCount + c);
-            p.chunkPrefix[c] = run;
-            run += x;
-            const bool lastOfView = SINGLE ? (c + 1 == n) : (c + 1 == ns);
-            if (lastOfView) {
-                const BatchViewDev& bv = view_of<SINGLE>(p, v);
-                *bv.drawCount = run;
-                if (run > bv.capacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
+                p.chunkPrefix[c] = run;
+                run += x[u];
+                const bool lastOfView = SINGLE ? (c + 1 == n) : (c + 1 == ns);
+                if (lastOfView) {
+                    const BatchViewDev& bv = view_of<SINGLE>(p, v);
+                    *bv.drawCount = run;
+                    if (run > bv.capacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
+                }
             }
         }
     }
@@ -323,7 +327,7 @@ __device__ __forceinline__ void scan_chunk_counts(const PipeParams& p, uint32_t*
 // ------------------------------------------------------------------ decide kernel
 
 template <int MODE, bool SINGLE, int THREADS, int OPT>
-__global__ void __launch_bounds__(THREADS) cull_decide_kernel(const PipeParams p) {
+__global__ void __launch_bounds__(THREADS, SINGLE ? 1024 / THREADS : 1) cull_decide_kernel(const PipeParams p) {
     constexpr int NW = THREADS / 32;
     __shared__ uint32_t s_sum[NW], s_flag[NW];
     __shared__ int s_last;
@@ -346,13 +350,13 @@ __global__ void __launch_bounds__(THREADS) cull_decide_kernel(const PipeParams p
         uint32_t total = 0;
         if (MODE == kModeRuntime) {
             switch (bv.mode) {
-                case BLZ_MODE_FIRST: total = decide_run_warp<BLZ_MODE_FIRST, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
-                case BLZ_MODE_LATE: total = decide_run_warp<BLZ_MODE_LATE, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
-                case BLZ_MODE_TEMPORAL: total = decide_run_warp<BLZ_MODE_TEMPORAL, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
-                default: total = decide_run_warp<BLZ_MODE_FRUSTUM, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
+                case BLZ_MODE_FIRST: total = decide_run_warp<BLZ_MODE_FIRST, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
+                case BLZ_MODE_LATE: total = decide_run_warp<BLZ_MODE_LATE, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
+                case BLZ_MODE_TEMPORAL: total = decide_run_warp<BLZ_MODE_TEMPORAL, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
+                default: total = decide_run_warp<BLZ_MODE_FRUSTUM, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
             }
         } else {
-            total = decide_run_warp<(MODE < 0 ? 0 : MODE), OPT>(p.sc, bv, base, limit, stage, ring, flags);
+            total = decide_run_warp<(MODE < 0 ? 0 : MODE), SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, flags);
         }
         if (lane == 0) p.chunkCount[chunk] = total;
     }
