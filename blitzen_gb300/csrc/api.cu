@@ -102,7 +102,7 @@ int ensure_chunk_scratch(blz_ctx* c, size_t chunks, size_t chunkSize) {
         c->chunkMem = nullptr;
         c->chunkObjects = c->chunkSlots = 0;
     }
-    const size_t bytes = wantObj * sizeof(uint2) + 2 * wantSlots * sizeof(uint32_t) + 256;
+    const size_t bytes = wantObj * sizeof(uint2) + wantSlots * sizeof(uint32_t) + 256;
     if (cudaMalloc(&c->chunkMem, bytes) != cudaSuccess) return fail(BLZ_ERR_OUT_OF_MEMORY, "object-cull scratch of %zu bytes", bytes);
     c->chunkObjects = wantObj;
     c->chunkSlots = wantSlots;
@@ -113,8 +113,6 @@ void bind_chunk_scratch(blz_ctx* c, PipeParams& p) {
     char* m = static_cast<char*>(c->chunkMem);
     p.staged = reinterpret_cast<uint2*>(m);
     p.chunkCount = reinterpret_cast<uint32_t*>(m + c->chunkObjects * sizeof(uint2));
-    p.chunkPrefix = p.chunkCount + c->chunkSlots;
-    p.doneBlocks = c->pyrCounter + 1;
     p.scratch = c->scratch;
 }
 

@@ -31,7 +31,7 @@ struct blz_ctx {
     size_t stagingBytes = 0;
     void* batchDev = nullptr;          // device BatchViewDev[] + tileStart[]
     size_t batchBytes = 0;
-    void* chunkMem = nullptr;          // object-cull staging: records, chunk counts, chunk prefixes
+    void* chunkMem = nullptr;          // object-cull staging: records, chunk counts
     size_t chunkObjects = 0;           // staged-record capacity
     size_t chunkSlots = 0;             // chunk count capacity
     bool hasScene = false;

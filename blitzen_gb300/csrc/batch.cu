@@ -304,15 +304,13 @@ int blz_batch_graph_create(blz_ctx* c, const BlzBatchView* views, uint32_t n, bl
     if (rc == BLZ_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = fail(BLZ_ERR_CUDA, "batch graph upload failed");
     if (rc == BLZ_OK) {
         const size_t chunks = ts[n], objects = chunks * tile;
-        const size_t bytes = objects * sizeof(uint2) + 2 * chunks * sizeof(uint32_t) + 256;
+        const size_t bytes = objects * sizeof(uint2) + chunks * sizeof(uint32_t) + 256;
         if (cudaMalloc(&g->chunkMem, bytes) != cudaSuccess || cudaMemset(g->chunkMem, 0, bytes) != cudaSuccess) {
             rc = fail(BLZ_ERR_OUT_OF_MEMORY, "batch graph scratch allocation failed");
         } else {
             char* m = static_cast<char*>(g->chunkMem);
             p.staged = reinterpret_cast<uint2*>(m);
             p.chunkCount = reinterpret_cast<uint32_t*>(m + objects * sizeof(uint2));
-            p.chunkPrefix = p.chunkCount + chunks;
-            p.doneBlocks = reinterpret_cast<unsigned int*>(p.chunkPrefix + chunks);
             p.scratch = c->scratch;
         }
     }

@@ -2,14 +2,13 @@
 // occlusion, for one view or many views in one launch.
 //
 // Two kernels per launch, no block ever waiting on another:
-//   decide   a streaming grid (several blocks per SM, grid-stride over 512-object chunks of all
-//            views) loads render objects and gathers their transforms with batched read-only loads,
-//            decides every object, ranks the emitted ones in ascending object order with warp
-//            ballots and a block scan, and stages them compacted — (objectId, lodId), 8 bytes — in
-//            the chunk's slice of a scratch buffer, with the chunk's count. The last block to
-//            finish scans the chunk counts per view (output offsets and draw counts).
-//   scatter  copies each chunk's staged records to their final slots as full indirect records,
-//            coalesced.
+//   decide   a streaming grid of warps, each deciding one contiguous chunk of a view's render
+//            objects (single views: one chunk per resident warp; batches: 512-object chunks of all
+//            views), stages the emitted ones compacted in object order — (objectId, lodId), 8 bytes —
+//            in the chunk's slice of a scratch buffer, and writes the chunk's count;
+//   scatter  one block per eight chunks: the block finds its chunks' output offsets from the counts
+//            (no grid-wide scan), copies the staged records to their final slots as full indirect
+//            records, and the owner of each view's last chunk writes the view's draw count.
 // The scratch traffic is 16 bytes per emitted object, against 40-48 bytes read per object.
 //
 // Reference passes (paths inside the Blitzen project):
@@ -217,120 +216,11 @@ __device__ __forceinline__ void put_record(uint8_t* cmds, uint32_t stride, uint3
     }
 }
 
-// Segmented exclusive scan of the chunk counts by one block, segments being the views: every
-// thread owns a contiguous run of chunks, sums it (loads of a run are independent, so a thread pays
-// about one L2 latency per eight chunks), the block scans the (sum, starts-a-segment) pairs, and
-// each thread rescans its run writing offsets and, at the end of a view, that view's draw count.
-template <bool SINGLE, int THREADS>
-__device__ __forceinline__ void scan_chunk_counts(const PipeParams& p, uint32_t* s_sum, uint32_t* s_flag) {
-    const uint32_t n = p.totalTiles;
-    const uint32_t runLen = (n + THREADS - 1) / THREADS;
-    const uint32_t r0 = min(n, threadIdx.x * runLen), r1 = min(n, r0 + runLen);
-    uint32_t vi = 0, nextStart = n;
-    if constexpr (!SINGLE) {
-        if (r0 < r1) {
-            vi = find_view(p.tileStart, p.viewCount, r0);
-            nextStart = __ldg(p.tileStart + vi + 1);
-        }
-    }
-    // pass 1: run sum since the last segment start inside the run
-    uint32_t sum = 0, hasStart = 0;
-    {
-        uint32_t v = vi, ns = nextStart;
-        for (uint32_t c = r0; c < r1; c += 8) {
-            uint32_t x[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) x[u] = (c + u < r1) ? __ldcg(p.chunkCount + c + u) : 0u;
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const uint32_t cc = c + u;
-                if (cc >= r1) break;
-                if constexpr (!SINGLE) {
-                    while (cc >= ns) {
-                        ++v;
-                        ns = __ldg(p.tileStart + v + 1);
-                    }
-                    if (cc == __ldg(p.tileStart + v)) {
-                        sum = 0;
-                        hasStart = 1;
-                    }
-                } else if (cc == 0) {
-                    sum = 0;
-                    hasStart = 1;
-                }
-                sum += x[u];
-            }
-        }
-    }
-    // block-wide segmented exclusive scan of (sum, hasStart): combine(a, b) = b.hasStart ? b : a + b
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    uint32_t isum = sum, iflag = hasStart;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t ps = __shfl_up_sync(0xFFFFFFFFu, isum, o);
-        const uint32_t pf = __shfl_up_sync(0xFFFFFFFFu, iflag, o);
-        if (lane >= static_cast<uint32_t>(o) && !iflag) {
-            isum += ps;
-            iflag = pf;
-        }
-    }
-    if (lane == 31) {
-        s_sum[warp] = isum;
-        s_flag[warp] = iflag;
-    }
-    __syncthreads();
-    // carry into this warp from the warps before it
-    uint32_t wsum = 0;
-    for (int w = 0; w < static_cast<int>(warp); ++w) wsum = s_flag[w] ? s_sum[w] : wsum + s_sum[w];
-    // exclusive carry for this thread = inclusive of previous lanes (within warp) combined with wsum
-    uint32_t prevSum = __shfl_up_sync(0xFFFFFFFFu, isum, 1);
-    uint32_t prevFlag = __shfl_up_sync(0xFFFFFFFFu, iflag, 1);
-    if (lane == 0) {
-        prevSum = 0;
-        prevFlag = 0;
-    }
-    uint32_t carry = prevFlag ? prevSum : wsum + prevSum;
-    // pass 2: offsets, and each view's total at its last chunk (counts fetched eight at a time, so a
-    // run costs one L2 latency per eight chunks here too)
-    {
-        uint32_t v = vi, ns = nextStart, run = carry;
-        for (uint32_t c0 = r0; c0 < r1; c0 += 8) {
-            uint32_t x[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) x[u] = (c0 + u < r1) ? __ldcg(p.chunkCount + c0 + u) : 0u;
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const uint32_t c = c0 + u;
-                if (c >= r1) break;
-                if constexpr (!SINGLE) {
-                    while (c >= ns) {
-                        ++v;
-                        ns = __ldg(p.tileStart + v + 1);
-                    }
-                    if (c == __ldg(p.tileStart + v)) run = 0;
-                } else if (c == 0) {
-                    run = 0;
-                }
-                p.chunkPrefix[c] = run;
-                run += x[u];
-                const bool lastOfView = SINGLE ? (c + 1 == n) : (c + 1 == ns);
-                if (lastOfView) {
-                    const BatchViewDev& bv = view_of<SINGLE>(p, v);
-                    *bv.drawCount = run;
-                    if (run > bv.capacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
-                }
-            }
-        }
-    }
-}
-
 // ------------------------------------------------------------------ decide kernel
 
 template <int MODE, bool SINGLE, int THREADS, int OPT>
 __global__ void __launch_bounds__(THREADS, SINGLE ? 1024 / THREADS : 1) cull_decide_kernel(const PipeParams p) {
     constexpr int NW = THREADS / 32;
-    __shared__ uint32_t s_sum[NW], s_flag[NW];
-    __shared__ int s_last;
     __shared__ __align__(16) Survivor s_ring[NW][kRing];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t warpsTotal = gridDim.x * NW;
@@ -361,40 +251,74 @@ __global__ void __launch_bounds__(THREADS, SINGLE ? 1024 / THREADS : 1) cull_dec
         if (lane == 0) p.chunkCount[chunk] = total;
     }
     if (flags) atomicOr(&p.scratch->status, flags);
-
-    // the last block to finish turns the chunk counts into per-view output offsets and draw counts
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = (atomicAdd(p.doneBlocks, 1u) == gridDim.x - 1u) ? 1 : 0;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    scan_chunk_counts<SINGLE, THREADS>(p, s_sum, s_flag);
-    if (threadIdx.x == 0) *p.doneBlocks = 0u;
 }
 
 // ------------------------------------------------------------------ scatter kernel
 
-// Each warp copies one chunk's staged records to their final slots as full records.
+// Each block owns kScatterWarps consecutive chunks, one per warp. It finds where its chunks' records
+// go without any grid-wide step: the block sums the counts of its first chunk's view that precede
+// that chunk (a strided read of at most one view's counts, from L2), then scans its own chunks'
+// counts (restarting at view boundaries). Each warp then copies its chunk's staged records to their
+// slots as full records, and the warp holding a view's last chunk writes that view's draw count.
+constexpr int kScatterWarps = 8;
+
 template <bool SINGLE>
-__global__ void __launch_bounds__(256) cull_scatter_kernel(const PipeParams p) {
+__global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const PipeParams p) {
+    __shared__ uint32_t s_part[kScatterWarps];
+    __shared__ uint32_t s_base[kScatterWarps];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t chunkSize = p.chunkSize;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t warpsTotal = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t chunk = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); chunk < p.totalTiles; chunk += warpsTotal) {
-        const uint32_t n = __ldg(p.chunkCount + chunk);
-        if (n == 0) continue;
-        const uint32_t vi = SINGLE ? 0u : find_view(p.tileStart, p.viewCount, chunk);
-        const BatchViewDev& bv = view_of<SINGLE>(p, vi);
-        const uint32_t base = __ldg(p.chunkPrefix + chunk);
-        const uint2* stage = p.staged + static_cast<size_t>(chunk) * chunkSize;
-        for (uint32_t j = lane; j < n; j += 32) {
-            const uint32_t slot = base + j;
-            if (slot >= bv.capacity) break;
-            const uint2 rec = __ldg(stage + j);
-            const uint2 lod = __ldg(reinterpret_cast<const uint2*>(p.sc.lods + rec.y));  // indexCount, firstIndex
-            put_record(bv.cmds, bv.stride, slot, rec.x, lod.x, lod.y);
+    const uint32_t c0 = blockIdx.x * kScatterWarps;
+    if (c0 >= p.totalTiles) return;
+    const uint32_t vi0 = SINGLE ? 0u : find_view(p.tileStart, p.viewCount, c0);
+    const uint32_t viewStart0 = SINGLE ? 0u : __ldg(p.tileStart + vi0);
+    // 1. records of the first chunk's view before c0
+    uint32_t part = 0;
+    for (uint32_t c = viewStart0 + threadIdx.x; c < c0; c += kScatterWarps * 32) part += __ldcg(p.chunkCount + c);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
+    if (lane == 0) s_part[warp] = part;
+    __syncthreads();
+    // 2. exclusive offsets of this block's chunks, restarting at each view's first chunk
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int w = 0; w < kScatterWarps; ++w) run += s_part[w];
+        uint32_t vNext = SINGLE ? p.totalTiles : __ldg(p.tileStart + vi0 + 1);
+        uint32_t vi = vi0;
+        for (int w = 0; w < kScatterWarps; ++w) {
+            const uint32_t c = c0 + w;
+            if (c >= p.totalTiles) break;
+            if constexpr (!SINGLE) {
+                while (c >= vNext) {  // a new view starts at c
+                    ++vi;
+                    vNext = __ldg(p.tileStart + vi + 1);
+                    run = 0;
+                }
+            }
+            s_base[w] = run;
+            run += __ldcg(p.chunkCount + c);
         }
+    }
+    __syncthreads();
+    // 3. scatter; the last chunk of a view writes its draw count
+    const uint32_t chunk = c0 + warp;
+    if (chunk >= p.totalTiles) return;
+    const uint32_t vi = SINGLE ? 0u : find_view(p.tileStart, p.viewCount, chunk);
+    const BatchViewDev& bv = view_of<SINGLE>(p, vi);
+    const uint32_t n = __ldcg(p.chunkCount + chunk);
+    const uint32_t base = s_base[warp];
+    const bool lastOfView = SINGLE ? (chunk + 1 == p.totalTiles) : (chunk + 1 == __ldg(p.tileStart + vi + 1));
+    if (lastOfView && lane == 0) {
+        *bv.drawCount = base + n;
+        if (base + n > bv.capacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
+    }
+    const uint2* stage = p.staged + static_cast<size_t>(chunk) * chunkSize;
+    for (uint32_t j = lane; j < n; j += 32) {
+        const uint32_t slot = base + j;
+        if (slot >= bv.capacity) break;
+        const uint2 rec = __ldcg(stage + j);
+        const uint2 lod = __ldg(reinterpret_cast<const uint2*>(p.sc.lods + rec.y));  // indexCount, firstIndex
+        put_record(bv.cmds, bv.stride, slot, rec.x, lod.x, lod.y);
     }
 }
 
@@ -427,11 +351,8 @@ static cudaError_t launch_t(const PipeParams& p, uint32_t blocksPerSm, int smCou
     kern<<<grid, THREADS, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    uint32_t sgrid = (p.totalTiles + 7) / 8;  // one warp per chunk
-    const uint32_t maxGrid = 16u * static_cast<uint32_t>(smCount);
-    if (sgrid > maxGrid) sgrid = maxGrid;
-    if (sgrid == 0) sgrid = 1;
-    cull_scatter_kernel<SINGLE><<<sgrid, 256, 0, s>>>(p);
+    const uint32_t sgrid = (p.totalTiles + kScatterWarps - 1) / kScatterWarps;  // one warp per chunk
+    cull_scatter_kernel<SINGLE><<<sgrid ? sgrid : 1u, kScatterWarps * 32, 0, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -73,7 +73,8 @@ struct BatchViewDev {
 
 // Parameters of the object-cull kernels: one view inline (single-view launches) or an array of
 // views in device memory with the first chunk of each (viewCount + 1 entries), plus the scratch
-// the decide kernel stages compacted records in (chunk c owns staged[c * chunkSize ...]).
+// the decide kernel stages compacted records in (chunk c owns staged[c * chunkSize ...]) and the
+// per-chunk record counts the scatter kernel turns into output offsets.
 struct PipeParams {
     SceneT sc;
     BatchViewDev single;
@@ -86,8 +87,6 @@ struct PipeParams {
     Scratch* scratch;      // status word
     uint2* staged;         // [totalTiles * chunkSize] (objectId, lodId)
     uint32_t* chunkCount;  // [totalTiles]
-    uint32_t* chunkPrefix; // [totalTiles]
-    unsigned int* doneBlocks;
 };
 
 struct InstancedParams {

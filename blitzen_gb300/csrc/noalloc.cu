@@ -1,21 +1,20 @@
 // noalloc.cu — blz_cull_frustum_noalloc: the frustum + LOD cull with its per-call staging held in
 // a fixed array of this library's own device memory, so the call allocates nothing.
 //
-// blz_cull_frustum stages each chunk's emitted (object, LOD) pairs, the chunk counts, the chunk
-// prefixes and a done-blocks counter in context memory that grows on demand, and growing it means
-// cudaFree + cudaMalloc. Some callers cannot take that: a frame loop that has reserved all of its
+// blz_cull_frustum stages each chunk's emitted (object, LOD) pairs and the chunk counts in context
+// memory that grows on demand, and growing it means cudaFree + cudaMalloc. Some callers cannot take that: a frame loop that has reserved all of its
 // device memory up front (another pool owns the rest, so a cudaMalloc would fail mid-frame), or
 // one that must never stall, since cudaFree waits for the whole device. This entry point runs the
 // same two kernels with that staging in `g_noallocScratch` below, a file-scope array sized for at
 // most BLZ_NOALLOC_MAX_OBJECTS render objects, and rejects larger lists instead of growing.
 //
 // Set-up: the array's device address is fetched with cudaGetSymbolAddress once per device, by
-// the first call made with that device current, and the done-blocks counter is cleared there
-// with a blocking cudaMemset. That first call therefore has to come before any stream capture.
+// the first call made with that device current. Make that first call before any stream capture.
 // After set-up a call only validates its arguments and launches.
 //
-// Only the done-blocks counter must start at zero; the decide kernel's last block puts it back
-// to zero at the end of every call. Every other word is written before it is read in each call.
+// Nothing in the array has to start at zero: each call writes every word it later reads (each
+// chunk's count and staged records are written by the decide kernel before the scatter kernel
+// reads them).
 //
 // The array is one per device for the whole process, shared by every context on that device:
 // two calls that overlap on the device (two streams, two threads, two contexts) race on it and
@@ -32,13 +31,11 @@ constexpr uint32_t kNoAllocChunk = 512;  // objects per chunk (the kernels take 
 constexpr uint32_t kNoAllocChunks = BLZ_NOALLOC_MAX_OBJECTS / kNoAllocChunk;
 static_assert(BLZ_NOALLOC_MAX_OBJECTS % kNoAllocChunk == 0, "the object bound must be whole chunks");
 
-// layout: staged records | chunk counts | chunk prefixes | done-blocks counter (own 256-byte line)
+// layout: staged records | chunk counts
 constexpr size_t kStagedBytes = size_t(BLZ_NOALLOC_MAX_OBJECTS) * sizeof(uint2);
 constexpr size_t kCountsOffset = kStagedBytes;
-constexpr size_t kPrefixOffset = kCountsOffset + size_t(kNoAllocChunks) * sizeof(uint32_t);
-constexpr size_t kDoneOffset = kPrefixOffset + size_t(kNoAllocChunks) * sizeof(uint32_t);
-constexpr size_t kNoAllocBytes = kDoneOffset + 256;
-static_assert(kPrefixOffset % 256 == 0 && kDoneOffset % 256 == 0, "regions start on 256-byte lines");
+constexpr size_t kNoAllocBytes = kCountsOffset + size_t(kNoAllocChunks) * sizeof(uint32_t);
+static_assert(kCountsOffset % 256 == 0, "regions start on 256-byte lines");
 
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
 
@@ -54,8 +51,6 @@ int scratch_base(int device, unsigned char** out) {
         cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress of the no-alloc scratch");
         if (reinterpret_cast<uintptr_t>(p) % 256 != 0) return fail(BLZ_ERR_CUDA, "no-alloc scratch is not 256-byte aligned");
-        e = cudaMemset(static_cast<unsigned char*>(p) + kDoneOffset, 0, sizeof(unsigned int));
-        if (e != cudaSuccess) return cuda_fail(e, "clearing the no-alloc done counter");
         g_base[device] = static_cast<unsigned char*>(p);
     }
     *out = g_base[device];
@@ -103,8 +98,6 @@ extern "C" int blz_cull_frustum_noalloc(blz_ctx* c, const BlzCameraViewData* vie
     p.scratch = c->scratch;  // status flags stay in the context, read by blz_ctx_check
     p.staged = reinterpret_cast<uint2*>(base);
     p.chunkCount = reinterpret_cast<uint32_t*>(base + kCountsOffset);
-    p.chunkPrefix = reinterpret_cast<uint32_t*>(base + kPrefixOffset);
-    p.doneBlocks = reinterpret_cast<unsigned int*>(base + kDoneOffset);
     e = launch_object_cull(BLZ_MODE_FRUSTUM, p, c->singleThreads, c->singleOpt, c->smCount,
                            reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "no-alloc cull launch");

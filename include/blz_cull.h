@@ -82,7 +82,7 @@ int blz_ctx_destroy(blz_ctx* ctx);
 /* Message of the last failing call made on this thread ("" if none). */
 const char* blz_last_error(void);
 
-/* Library version string and the number of kernels this build contains. */
+/* Library version string (name, version, target architecture). */
 const char* blz_version(void);
 
 /* Synchronises the stream, returns the device status flags raised since the last check and
@@ -197,8 +197,8 @@ int blz_cull_frustum(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList 
  * up front, or they must not wait on the device-wide synchronisation of cudaFree). Its per-call
  * staging is a fixed device array inside this library, for at most BLZ_NOALLOC_MAX_OBJECTS render
  * objects (8 MiB); longer lists return BLZ_ERR_CAPACITY. Results equal blz_cull_frustum's.
- * The first call with a device current fetches that array's address and clears its counter
- * (a blocking cudaMemset), so make it before any stream capture. The array is shared by every
+ * The first call with a device current fetches that array's address (cudaGetSymbolAddress), so
+ * make it before any stream capture. The array is shared by every
  * context on the device: calls that overlap on the device race on it and must be ordered. */
 #define BLZ_NOALLOC_MAX_OBJECTS (1u << 20)
 int blz_cull_frustum_noalloc(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
