@@ -8,7 +8,9 @@ LODs; one step is one occlusion frame of the reference's D3D12 path (dx12Draw.cp
 Inputs are resident in HBM when the timed region starts; before each step the visibility buffer is
 restored to the 50% mask and L2 is flushed (a 512 MiB read), both outside the timed events.
 
-value  = objects per second of the device-timed frames (sum of per-step CUDA-event times).
+value  = objects per second of the device-timed frames: each step replays the frame (the three passes,
+         recorded once with blz_capture_begin/end) as one CUDA graph between two CUDA events; the
+         per-pass breakdown in `roofline` replays each pass as its own graph.
 e2e    = the same frame through the C ABI with host buffers: per step the depth buffer (8.3 MB) and
          the 1,000 dynamic transforms are copied from pinned host memory and both draw counts are
          read back, all inside the timed region.
@@ -231,21 +233,31 @@ def main():
         V1, _ = t1.read()
         V2, _ = t2.read()
         # the frame as three recorded passes, replayed back to back (no host work between kernels)
-        graphs = []
+        # the frame (pass 1, pyramid, pass 2) recorded once and replayed as one graph per step; the
+        # three passes are also recorded one by one for the per-pass breakdown
+        c.capture_begin()
+        step_direct()
+        frame = c.capture_end()
+        kernels_per_step = frame.kernels
+        passes = []
         for fn in (lambda: c.draw_cull_first_pass(v, vis, t1), lambda: c.generate_depth_pyramid(pyr, depth),
                    lambda: c.draw_cull_occlusion_pass(v, vis, pyr, t2)):
             c.capture_begin()
             fn()
-            graphs.append(c.capture_end())
-        kernels_per_step = sum(g.kernels for g in graphs)
+            passes.append(c.capture_end())
 
         def step(e=None):
-            for j, g in enumerate(graphs):
-                if e:
-                    e[j].record()
-                g.launch()
             if e:
-                e[3].record()
+                e[0].record()
+            frame.launch()
+            if e:
+                e[1].record()
+
+        def step_passes(e):
+            for j, g in enumerate(passes):
+                e[j].record()
+                g.launch()
+            e[3].record()
 
         for _ in range(max(args.warmup, 3)):
             vis.copy_(vis0)
@@ -271,11 +283,18 @@ def main():
                     flush_l2()
                     step()
                 side.synchronize()
+        # per-pass breakdown (not part of the headline): each pass replayed as its own graph
+        evp = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+        for k in range(args.steps):
+            vis.copy_(vis0)
+            flush_l2()
+            step_passes(evp[k])
+        side.synchronize()
     c.check()
-    ms = [(e[0].elapsed_time(e[3])) for e in ev]
-    ms_first = [e[0].elapsed_time(e[1]) for e in ev]
-    ms_pyr = [e[1].elapsed_time(e[2]) for e in ev]
-    ms_late = [e[2].elapsed_time(e[3]) for e in ev]
+    ms = [(e[0].elapsed_time(e[1])) for e in ev]
+    ms_first = [e[0].elapsed_time(e[1]) for e in evp]
+    ms_pyr = [e[1].elapsed_time(e[2]) for e in evp]
+    ms_late = [e[2].elapsed_time(e[3]) for e in evp]
     t_step = sum(ms) / len(ms)
     if world > 1:
         tt = torch.tensor([t_step], device=dev)

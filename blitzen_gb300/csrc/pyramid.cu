@@ -2,9 +2,10 @@
 //
 // The reference builds the pyramid with one dispatch per mip and a barrier between them
 // (src/Renderer/BlitzenDX12/dx12Draw.cpp:248-277, src/Renderer/BlitzenVulkan/vulkanDraw.cpp:579-614).
-// Here one launch builds every mip: each block owns a 64x64 tile of mip 0, writes it, and reduces
-// it through mips 1..6 in shared memory (a 64-texel tile reaches 1 texel at mip 6); the last block
-// to finish (device counter) builds the few remaining small mips from mip 6 in global memory.
+// Here one launch builds every mip: each block owns a 32x32 tile of mip 0 (every load of the tile
+// issued before any is used), writes it, and reduces it through mips 1..5 in shared memory (a
+// 32-texel tile reaches 1 texel at mip 5); the last block to finish (device counter) reads mip 5
+// into shared memory when it fits and builds the few remaining small mips there.
 //
 // Texel rules:
 //   D3D12   depthPyramid.cs.hlsl:16-26 — min(r, min(g, min(b, a))) of the 2x2 Loads at
@@ -20,8 +21,10 @@
 namespace blz {
 
 constexpr int kPyrThreads = 256;
-constexpr uint32_t kPyrTile = 64;
-constexpr uint32_t kPyrInTileLevels = 6;
+constexpr uint32_t kPyrTile = 32;
+constexpr uint32_t kPyrInTileLevels = 5;
+constexpr uint32_t kPyrPerThread = kPyrTile * kPyrTile / kPyrThreads;  // mip-0 texels per thread
+constexpr uint32_t kPyrTopTexels = 4096;  // the last block keeps the upper levels in shared memory up to this
 
 __device__ __forceinline__ float load_or_zero(const float* img, uint32_t w, uint32_t h, uint64_t x, uint64_t y) {
     return (x < w && y < h) ? __ldcg(img + y * w + x) : 0.0f;
@@ -71,24 +74,51 @@ template <uint32_t MODE>
 __global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuildParams p) {
     __shared__ float sA[kPyrTile * kPyrTile];
     __shared__ float sB[(kPyrTile / 2) * (kPyrTile / 2)];
+    __shared__ float sTop[2][kPyrTopTexels];
     __shared__ int s_last;
     const uint32_t X0 = blockIdx.x * kPyrTile, Y0 = blockIdx.y * kPyrTile;
     const uint32_t W0 = p.width, H0 = p.height;
 
-    // mip 0 from the depth buffer
-    for (uint32_t idx = threadIdx.x; idx < kPyrTile * kPyrTile; idx += kPyrThreads) {
-        const uint32_t lx = idx & (kPyrTile - 1), ly = idx / kPyrTile;
-        const uint32_t gx = X0 + lx, gy = Y0 + ly;
-        float v = 0.0f;
-        if (gx < W0 && gy < H0) {
-            v = level_texel_global<MODE>(p.depth, p.depthWidth, p.depthHeight, gx, gy, W0, H0);
-            p.data[p.mipOffset[0] + static_cast<size_t>(gy) * W0 + gx] = v;
+    // mip 0 from the depth buffer: all of a thread's source loads are in flight together
+    {
+        float v[kPyrPerThread];
+        if (MODE == BLZ_HIZ_D3D12) {
+            float q[kPyrPerThread][4];
+#pragma unroll
+            for (uint32_t j = 0; j < kPyrPerThread; ++j) {
+                const uint32_t idx = threadIdx.x + j * kPyrThreads;
+                const uint32_t gx = X0 + (idx % kPyrTile), gy = Y0 + (idx / kPyrTile);
+                const bool in = gx < W0 && gy < H0;
+                const uint64_t x0 = 2ull * gx, y0 = 2ull * gy;
+                const uint32_t dw = p.depthWidth, dh = p.depthHeight;
+                q[j][0] = (in && x0 < dw && y0 < dh) ? __ldg(p.depth + y0 * dw + x0) : 0.0f;
+                q[j][1] = (in && x0 + 1 < dw && y0 < dh) ? __ldg(p.depth + y0 * dw + x0 + 1) : 0.0f;
+                q[j][2] = (in && x0 < dw && y0 + 1 < dh) ? __ldg(p.depth + (y0 + 1) * dw + x0) : 0.0f;
+                q[j][3] = (in && x0 + 1 < dw && y0 + 1 < dh) ? __ldg(p.depth + (y0 + 1) * dw + x0 + 1) : 0.0f;
+            }
+#pragma unroll
+            for (uint32_t j = 0; j < kPyrPerThread; ++j) v[j] = fmin_nan(q[j][0], fmin_nan(q[j][1], fmin_nan(q[j][2], q[j][3])));
+        } else {
+#pragma unroll
+            for (uint32_t j = 0; j < kPyrPerThread; ++j) {
+                const uint32_t idx = threadIdx.x + j * kPyrThreads;
+                const uint32_t gx = X0 + (idx % kPyrTile), gy = Y0 + (idx / kPyrTile);
+                v[j] = (gx < W0 && gy < H0) ? level_texel_global<MODE>(p.depth, p.depthWidth, p.depthHeight, gx, gy, W0, H0)
+                                            : 0.0f;
+            }
         }
-        sA[idx] = v;
+#pragma unroll
+        for (uint32_t j = 0; j < kPyrPerThread; ++j) {
+            const uint32_t idx = threadIdx.x + j * kPyrThreads;
+            const uint32_t gx = X0 + (idx % kPyrTile), gy = Y0 + (idx / kPyrTile);
+            const bool in = gx < W0 && gy < H0;
+            if (in) p.data[p.mipOffset[0] + static_cast<size_t>(gy) * W0 + gx] = v[j];
+            sA[idx] = in ? v[j] : 0.0f;
+        }
     }
     __syncthreads();
 
-    // mips 1..6 inside the tile
+    // mips 1..5 inside the tile
     float* src = sA;
     float* dst = sB;
     uint32_t S = kPyrTile;  // previous level's tile extent
@@ -145,7 +175,51 @@ __global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuild
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    for (uint32_t k = kPyrInTileLevels + 1; k < p.mipCount; ++k) {
+    uint32_t k = kPyrInTileLevels + 1;
+    {
+        // the level every tile finished, then the rest in shared memory while they fit
+        const uint32_t Wt = mip_dim(W0, kPyrInTileLevels), Ht = mip_dim(H0, kPyrInTileLevels);
+        if (Wt * Ht <= kPyrTopTexels) {
+            const float* top = p.data + p.mipOffset[kPyrInTileLevels];
+            for (uint32_t i = threadIdx.x; i < Wt * Ht; i += kPyrThreads) sTop[0][i] = __ldcg(top + i);
+            __syncthreads();
+            int cur = 0;
+            for (; k < p.mipCount; ++k) {
+                const uint32_t Wp = mip_dim(W0, k - 1), Hp = mip_dim(H0, k - 1);
+                const uint32_t Wk = mip_dim(W0, k), Hk = mip_dim(H0, k);
+                const float* prev = sTop[cur];
+                float* next = sTop[cur ^ 1];
+                float* out = p.data + p.mipOffset[k];
+                for (uint32_t idx = threadIdx.x; idx < Wk * Hk; idx += kPyrThreads) {
+                    const uint32_t gx = idx % Wk, gy = idx / Wk;
+                    float t;
+                    if (MODE == BLZ_HIZ_D3D12) {
+                        const uint32_t x0 = 2u * gx, y0 = 2u * gy;
+                        const float r = (x0 < Wp && y0 < Hp) ? prev[y0 * Wp + x0] : 0.0f;
+                        const float g = (x0 + 1 < Wp && y0 < Hp) ? prev[y0 * Wp + x0 + 1] : 0.0f;
+                        const float b = (x0 < Wp && y0 + 1 < Hp) ? prev[(y0 + 1) * Wp + x0] : 0.0f;
+                        const float a = (x0 + 1 < Wp && y0 + 1 < Hp) ? prev[(y0 + 1) * Wp + x0 + 1] : 0.0f;
+                        t = fmin_nan(r, fmin_nan(g, fmin_nan(b, a)));
+                    } else {
+                        uint32_t i0, i1, j0, j1;
+                        vk_footprint(gx, Wk, Wp, i0, i1);
+                        vk_footprint(gy, Hk, Hp, j0, j1);
+                        float m = __int_as_float(0x7fc00000);
+                        m = fmin_nan(m, prev[j0 * Wp + i0]);
+                        m = fmin_nan(m, prev[j0 * Wp + i1]);
+                        m = fmin_nan(m, prev[j1 * Wp + i0]);
+                        m = fmin_nan(m, prev[j1 * Wp + i1]);
+                        t = m;
+                    }
+                    next[idx] = t;
+                    out[idx] = t;
+                }
+                __syncthreads();
+                cur ^= 1;
+            }
+        }
+    }
+    for (; k < p.mipCount; ++k) {
         const uint32_t Wp = mip_dim(W0, k - 1), Hp = mip_dim(H0, k - 1);
         const uint32_t Wk = mip_dim(W0, k), Hk = mip_dim(H0, k);
         const float* prev = p.data + p.mipOffset[k - 1];
