@@ -113,6 +113,7 @@ void bind_chunk_scratch(blz_ctx* c, PipeParams& p) {
     char* m = static_cast<char*>(c->chunkMem);
     p.staged = reinterpret_cast<uint2*>(m);
     p.chunkCount = reinterpret_cast<uint32_t*>(m + c->chunkObjects * sizeof(uint2));
+    p.workCounter = c->pyrCounter + 1;  // [0] is the pyramid's
     p.scratch = c->scratch;
 }
 
@@ -453,6 +454,7 @@ static int object_cull(blz_ctx* c, uint32_t mode, const BlzCameraViewData* view,
     p.totalTiles = tiles;
     p.chunkSize = tile;
     bind_chunk_scratch(c, p);
+    p.workCounter = nullptr;  // one chunk per resident warp, assigned by warp index
     cudaError_t e = launch_object_cull(mode, p, c->singleThreads, c->singleOpt, c->smCount, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "cull launch");
     c->launches += 2;  // decide + scatter

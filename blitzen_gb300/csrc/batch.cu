@@ -311,6 +311,7 @@ int blz_batch_graph_create(blz_ctx* c, const BlzBatchView* views, uint32_t n, bl
             char* m = static_cast<char*>(g->chunkMem);
             p.staged = reinterpret_cast<uint2*>(m);
             p.chunkCount = reinterpret_cast<uint32_t*>(m + objects * sizeof(uint2));
+            p.workCounter = reinterpret_cast<unsigned int*>(p.chunkCount + chunks);  // zeroed above
             p.scratch = c->scratch;
         }
     }

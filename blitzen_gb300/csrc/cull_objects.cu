@@ -2,11 +2,12 @@
 // occlusion, for one view or many views in one launch.
 //
 // Two kernels per launch, no block ever waiting on another:
-//   decide   a streaming grid of warps, each deciding one contiguous chunk of a view's render
-//            objects (single views: one chunk per resident warp; batches: 512-object chunks of all
-//            views), stages the emitted ones compacted in object order — (objectId, lodId), 8 bytes —
-//            in the chunk's slice of a scratch buffer, and writes the chunk's count;
-//   scatter  one block per eight chunks: the block finds its chunks' output offsets from the counts
+//   decide   a streaming grid of warps, each deciding contiguous chunks of a view's render objects
+//            (single views: one chunk per resident warp, assigned by warp index; batches: 512-object
+//            chunks of all views, taken from a work counter), staging the emitted ones compacted in
+//            object order — (objectId, lodId), 8 bytes — in the chunk's slice of a scratch buffer,
+//            with the chunk's count;
+//   scatter  one block per 32 chunks: the block finds its chunks' output offsets from the counts
 //            (no grid-wide scan), copies the staged records to their final slots as full indirect
 //            records, and the owner of each view's last chunk writes the view's draw count.
 // The scratch traffic is 16 bytes per emitted object, against 40-48 bytes read per object.
@@ -226,7 +227,18 @@ __global__ void __launch_bounds__(THREADS, SINGLE ? 1024 / THREADS : 1) cull_dec
     const uint32_t warpsTotal = gridDim.x * NW;
     const uint32_t chunkSize = p.chunkSize;
     unsigned int flags = 0u;
-    for (uint32_t chunk = blockIdx.x * NW + warp; chunk < p.totalTiles; chunk += warpsTotal) {
+    // every warp starts on the chunk of its index; later chunks come from the work counter when
+    // there is one (a warp that finishes early takes the next, so warps finish together), else by
+    // a stride of the grid's warp count
+    auto next_chunk = [&](uint32_t cur) -> uint32_t {
+        if (p.workCounter == nullptr) return cur + warpsTotal;
+        uint32_t c = 0;
+        if (lane == 0) c = warpsTotal + atomicAdd(p.workCounter, 1u);
+        return __shfl_sync(0xFFFFFFFFu, c, 0);
+    };
+    uint32_t chunk = blockIdx.x * NW + warp;
+    while (chunk < p.totalTiles) {
+        const uint32_t next = next_chunk(chunk);  // asked now, used after this chunk
         uint32_t vi = 0, first = 0;
         if constexpr (!SINGLE) {
             vi = find_view(p.tileStart, p.viewCount, chunk);
@@ -249,26 +261,30 @@ __global__ void __launch_bounds__(THREADS, SINGLE ? 1024 / THREADS : 1) cull_dec
             total = decide_run_warp<(MODE < 0 ? 0 : MODE), SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, flags);
         }
         if (lane == 0) p.chunkCount[chunk] = total;
+        chunk = next;
     }
     if (flags) atomicOr(&p.scratch->status, flags);
 }
 
 // ------------------------------------------------------------------ scatter kernel
 
-// Each block owns kScatterWarps consecutive chunks, one per warp. It finds where its chunks' records
-// go without any grid-wide step: the block sums the counts of its first chunk's view that precede
-// that chunk (a strided read of at most one view's counts, from L2), then scans its own chunks'
-// counts (restarting at view boundaries). Each warp then copies its chunk's staged records to their
-// slots as full records, and the warp holding a view's last chunk writes that view's draw count.
-constexpr int kScatterWarps = 8;
+// Each block owns 32 consecutive chunks, one per warp, and finds where their records go without
+// any grid-wide step: it sums the counts of its first chunk's view that precede that chunk (a
+// strided read of at most one view's counts, from L2), and warp 0 scans the 32 chunks' counts
+// (restarting at view boundaries). The block's warps then copy the chunks' staged records to their slots as full
+// records, and the lane holding a view's last chunk writes that view's draw count. Block 0 also
+// rewinds the decide kernel's work counter for the next launch.
+constexpr int kScatterWarps = 32;  // one warp per chunk
+constexpr uint32_t kScatterChunks = 32;
 
 template <bool SINGLE>
 __global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const PipeParams p) {
     __shared__ uint32_t s_part[kScatterWarps];
-    __shared__ uint32_t s_base[kScatterWarps];
+    __shared__ uint32_t s_base[kScatterChunks], s_n[kScatterChunks], s_vi[kScatterChunks];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t chunkSize = p.chunkSize;
-    const uint32_t c0 = blockIdx.x * kScatterWarps;
+    const uint32_t c0 = blockIdx.x * kScatterChunks;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && p.workCounter != nullptr) *p.workCounter = 0u;
     if (c0 >= p.totalTiles) return;
     const uint32_t vi0 = SINGLE ? 0u : find_view(p.tileStart, p.viewCount, c0);
     const uint32_t viewStart0 = SINGLE ? 0u : __ldg(p.tileStart + vi0);
@@ -279,46 +295,63 @@ __global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const 
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
     if (lane == 0) s_part[warp] = part;
     __syncthreads();
-    // 2. exclusive offsets of this block's chunks, restarting at each view's first chunk
-    if (threadIdx.x == 0) {
-        uint32_t run = 0;
-        for (int w = 0; w < kScatterWarps; ++w) run += s_part[w];
-        uint32_t vNext = SINGLE ? p.totalTiles : __ldg(p.tileStart + vi0 + 1);
+    // 2. warp 0: exclusive offsets of the block's chunks, a scan restarting at each view's first chunk
+    if (warp == 0) {
+        uint32_t carry = 0;
+#pragma unroll
+        for (int w = 0; w < kScatterWarps; ++w) carry += s_part[w];
+        const uint32_t c = c0 + lane;
+        const bool in = c < p.totalTiles;
+        const uint32_t n = in ? __ldcg(p.chunkCount + c) : 0u;
         uint32_t vi = vi0;
-        for (int w = 0; w < kScatterWarps; ++w) {
-            const uint32_t c = c0 + w;
-            if (c >= p.totalTiles) break;
-            if constexpr (!SINGLE) {
-                while (c >= vNext) {  // a new view starts at c
-                    ++vi;
-                    vNext = __ldg(p.tileStart + vi + 1);
-                    run = 0;
-                }
+        bool starts = false;  // this chunk starts a view (the scan restarts here)
+        if constexpr (!SINGLE) {
+            if (in) {
+                vi = find_view(p.tileStart, p.viewCount, c);
+                starts = c == __ldg(p.tileStart + vi);
             }
-            s_base[w] = run;
-            run += __ldcg(p.chunkCount + c);
+        }
+        // segmented inclusive scan: combine(a, b) = b.starts ? b : a + b
+        uint32_t sum = n;
+        bool flag = starts;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t ps = __shfl_up_sync(0xFFFFFFFFu, sum, o);
+            const bool pf = __shfl_up_sync(0xFFFFFFFFu, flag ? 1u : 0u, o) != 0u;
+            if (lane >= static_cast<uint32_t>(o) && !flag) {
+                sum += ps;
+                flag = pf;
+            }
+        }
+        // lanes still in the first view (no start at or before them) add the view's earlier records
+        const uint32_t excl = sum - n + (flag ? 0u : carry);
+        s_base[lane] = excl;
+        s_n[lane] = n;
+        s_vi[lane] = vi;
+        if (in) {
+            const bool lastOfView = SINGLE ? (c + 1 == p.totalTiles) : (c + 1 == __ldg(p.tileStart + vi + 1));
+            if (lastOfView) {
+                const BatchViewDev& bv = view_of<SINGLE>(p, vi);
+                *bv.drawCount = excl + n;
+                if (excl + n > bv.capacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
+            }
         }
     }
     __syncthreads();
-    // 3. scatter; the last chunk of a view writes its draw count
-    const uint32_t chunk = c0 + warp;
-    if (chunk >= p.totalTiles) return;
-    const uint32_t vi = SINGLE ? 0u : find_view(p.tileStart, p.viewCount, chunk);
-    const BatchViewDev& bv = view_of<SINGLE>(p, vi);
-    const uint32_t n = __ldcg(p.chunkCount + chunk);
-    const uint32_t base = s_base[warp];
-    const bool lastOfView = SINGLE ? (chunk + 1 == p.totalTiles) : (chunk + 1 == __ldg(p.tileStart + vi + 1));
-    if (lastOfView && lane == 0) {
-        *bv.drawCount = base + n;
-        if (base + n > bv.capacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
-    }
-    const uint2* stage = p.staged + static_cast<size_t>(chunk) * chunkSize;
-    for (uint32_t j = lane; j < n; j += 32) {
-        const uint32_t slot = base + j;
-        if (slot >= bv.capacity) break;
-        const uint2 rec = __ldcg(stage + j);
-        const uint2 lod = __ldg(reinterpret_cast<const uint2*>(p.sc.lods + rec.y));  // indexCount, firstIndex
-        put_record(bv.cmds, bv.stride, slot, rec.x, lod.x, lod.y);
+    // 3. scatter, one chunk per warp at a time
+    for (uint32_t j = warp; j < kScatterChunks; j += kScatterWarps) {
+        const uint32_t chunk = c0 + j;
+        if (chunk >= p.totalTiles) break;
+        const uint32_t n = s_n[j], base = s_base[j];
+        const BatchViewDev& bv = view_of<SINGLE>(p, s_vi[j]);
+        const uint2* stage = p.staged + static_cast<size_t>(chunk) * chunkSize;
+        for (uint32_t i = lane; i < n; i += 32) {
+            const uint32_t slot = base + i;
+            if (slot >= bv.capacity) break;
+            const uint2 rec = __ldcg(stage + i);
+            const uint2 lod = __ldg(reinterpret_cast<const uint2*>(p.sc.lods + rec.y));  // indexCount, firstIndex
+            put_record(bv.cmds, bv.stride, slot, rec.x, lod.x, lod.y);
+        }
     }
 }
 
@@ -351,7 +384,7 @@ static cudaError_t launch_t(const PipeParams& p, uint32_t blocksPerSm, int smCou
     kern<<<grid, THREADS, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const uint32_t sgrid = (p.totalTiles + kScatterWarps - 1) / kScatterWarps;  // one warp per chunk
+    const uint32_t sgrid = (p.totalTiles + kScatterChunks - 1) / kScatterChunks;
     cull_scatter_kernel<SINGLE><<<sgrid ? sgrid : 1u, kScatterWarps * 32, 0, s>>>(p);
     return cudaGetLastError();
 }

@@ -87,6 +87,7 @@ struct PipeParams {
     Scratch* scratch;      // status word
     uint2* staged;         // [totalTiles * chunkSize] (objectId, lodId)
     uint32_t* chunkCount;  // [totalTiles]
+    unsigned int* workCounter;  // next chunk to decide (zero between launches), or NULL: static chunks
 };
 
 struct InstancedParams {
@@ -132,6 +133,8 @@ struct PyramidBuildParams {
 uint32_t object_tile_size();
 // Chunk size of a single-view launch of `count` objects: one chunk per warp the launch holds
 // resident, so every warp streams one contiguous run of objects and none waits for a second round.
+// (Smaller chunks handed out by a counter measured slower: each chunk drains its survivor ring in
+// a partial round, and thousands of warps contend for the counter.)
 uint32_t single_chunk_size(uint32_t mode, uint32_t threads, uint32_t opt, uint32_t count, int smCount);
 bool single_shape_supported(uint32_t threads, uint32_t opt);
 cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t threads, uint32_t opt, int smCount,
