@@ -322,14 +322,13 @@ def main():
                     "pyramid": {"ms": t_pyr, "bytes": bytes_pyr, "GB/s": bytes_pyr / (t_pyr * 1e-3) / 1e9},
                     "frame": {"ms": t_step, "bytes": bytes_first + bytes_pyr + bytes_late,
                               "GB/s": (bytes_first + bytes_pyr + bytes_late) / (t_step * 1e-3) / 1e9}}}
-    traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(traffic_file):
-        try:
-            with open(traffic_file) as f:
-                tr = json.load(f)
-            roofline["traffic"] = tr.get("cull_late_bytes_per_launch")
-        except Exception:
-            pass
+    # DRAM bytes of one pass-2 decide launch, from the ncu capture summarised in profiles/
+    prof = os.path.join(ROOT, "profiles", "cull_decide_late_4M.md")
+    if os.path.exists(prof) and args.objects == 4_000_000:
+        with open(prof) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    roofline["traffic"] = int(line.split(":")[1])
 
     # ---------------- e2e through the C ABI with host buffers
     hdepth = torch.empty(W * H, dtype=torch.float32, pin_memory=True)
