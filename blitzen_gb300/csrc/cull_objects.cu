@@ -104,7 +104,9 @@ __device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchVi
 // sb + k * 32 + lane for k < OPT, so lanes ascend within each 32-object slice):
 //   1  every lane loads its OPT render objects (fetched one step ahead) and their transforms and
 //      surfaces, and runs the frustum test — without branches: an object that is out of range,
-//      not active in this pass or has a bad id reads the tables' first rows and is masked out;
+//      not active in this pass or has a bad id reads the tables' first rows and is masked out.
+//      Pass 1 (single views) first packs the objects visible last frame into a candidate ring,
+//      so the frustum stage runs on full lanes there too;
 //   2  each slice's survivors are appended, in object order, to the warp's ring in shared memory;
 //      whenever 32 are waiting they go through the dense stage on full lanes, so the costly part
 //      (projection, Hi-Z, LOD) never runs on a lane without an object;
@@ -112,9 +114,10 @@ __device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchVi
 // Returns the number of records staged. No block barrier: warps never wait for one another.
 template <int MODE, bool SINGLE, int OPT>
 __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const BatchViewDev& bv, uint32_t base,
-                                                    uint32_t limit, uint2* stage, Survivor* ring,
+                                                    uint32_t limit, uint2* stage, Survivor* ring, uint4* cand,
                                                     unsigned int& flags) {
     constexpr uint32_t STEP = 32u * OPT;
+    constexpr bool PACK = (MODE == BLZ_MODE_FIRST) && SINGLE;  // candidate ring of 2 * STEP entries
     const uint32_t lane = threadIdx.x & 31u;
     if (sc.transformCount == 0u || sc.surfaceCount == 0u) {
         // nothing can be looked up: every object of the pass has a bad id and none is visible
@@ -127,6 +130,58 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
     }
     const ViewConsts v = load_view(bv.view);
     uint32_t run = 0, head = 0, tail = 0;
+
+    // frustum stage over OPT slices: obj[k] the object index, ro[k] its render object, vis[k] != 0
+    // when active (LATE: bit 31, with the previous visibility below it)
+    float4 ps[OPT], q[OPT], sph[OPT];
+    uint2 lod[OPT];
+    bool ok[OPT];
+    auto gather = [&](const uint2 (&ro)[OPT], const uint32_t (&vis)[OPT]) {
+#pragma unroll
+        for (int k = 0; k < OPT; ++k) {
+            ok[k] = vis[k] != 0u && ro[k].x < sc.transformCount && ro[k].y < sc.surfaceCount;
+            const uint32_t tid = ok[k] ? ro[k].x : 0u, sid = ok[k] ? ro[k].y : 0u;
+            const BlzMeshTransform* tt = sc.transforms;
+            if constexpr (!SINGLE) {
+                if (bv.dynT != nullptr && tid < bv.dynCount) tt = bv.dynT;
+            }
+            const float4* tp = reinterpret_cast<const float4*>(tt + tid);
+            const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + sid);
+            ps[k] = __ldg(tp);
+            q[k] = __ldg(tp + 1);
+            sph[k] = __ldg(sp);
+            const uint4 s1 = __ldg(reinterpret_cast<const uint4*>(sp + 1));  // materialId, lodOffset, lodCount, vertexOffset
+            lod[k] = make_uint2(s1.y, s1.z);
+        }
+    };
+    auto test = [&](const uint32_t (&obj)[OPT], const uint32_t (&vis)[OPT]) {
+#pragma unroll
+        for (int k = 0; k < OPT; ++k) {
+            const bool act = vis[k] != 0u;
+            const bool lodOk = lod[k].x < sc.lodCount && lod[k].y <= sc.lodCount - lod[k].x;
+            const bool good = ok[k] && lodOk;
+            if (act && !good) flags |= BLZ_FLAG_BAD_INDEX;
+            const Vec3 c = view_transform(v.rows, model_to_world(Vec3{sph[k].x, sph[k].y, sph[k].z}, ps[k], q[k]));
+            const float r = BLZ_FM(sph[k].w, ps[k].w);
+            const bool inFrustum = good && frustum_check(c, r, v);
+            if (MODE == BLZ_MODE_LATE && act && !inFrustum) bv.vis[obj[k]] = 0u;  // drawOccLate.cs.hlsl:67
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, inFrustum);
+            if (inFrustum) {
+                uint4* e = reinterpret_cast<uint4*>(ring + ((tail + __popc(m & lanemask_lt())) & (kRing - 1u)));
+                const uint32_t tag = (MODE == BLZ_MODE_LATE && (vis[k] & 0x7FFFFFFFu) != 0u) ? 0x80000000u : 0u;
+                e[0] = make_uint4(obj[k] | tag, __float_as_uint(c.x), __float_as_uint(c.y), __float_as_uint(c.z));
+                e[1] = make_uint4(__float_as_uint(r), __float_as_uint(ps[k].w), lod[k].x, lod[k].y);
+            }
+            tail += __popc(m);
+            if (tail - head >= 32u) {
+                __syncwarp();
+                dense_round<MODE>(sc, bv, v, ring, head, 32u, stage, run);
+                head += 32u;
+                __syncwarp();
+            }
+        }
+    };
+
     uint2 nro[OPT];
     uint32_t nvis[OPT];
     auto prefetch = [&](uint32_t at) {
@@ -140,58 +195,55 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
             if (MODE == BLZ_MODE_LATE && in) nvis[k] = bv.vis[i] | 0x80000000u;  // rewritten later by this warp: coherent load
         }
     };
+    // candidates packed by pass 1, taken STEP at a time (or the rest, at the end)
+    uint32_t ahead = 0, atail = 0;
+    auto take_candidates = [&](uint32_t n) {
+        uint2 ro[OPT];
+        uint32_t obj[OPT], vis[OPT];
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < OPT; ++k) {
+            const uint32_t j = k * 32u + lane;
+            const uint4 e = cand[(ahead + j) & (2u * STEP - 1u)];
+            const bool in = j < n;
+            obj[k] = e.x;
+            ro[k] = make_uint2(e.y, e.z);
+            vis[k] = in ? 1u : 0u;
+        }
+        __syncwarp();
+        ahead += n;
+        gather(ro, vis);
+        test(obj, vis);
+    };
+
     if (base < limit) prefetch(base);
     for (uint32_t sb = base; sb < limit; sb += STEP) {
-        uint32_t visPrev[OPT];
-        bool act[OPT], ok[OPT];
-        float4 ps[OPT], q[OPT], sph[OPT];
-        uint2 lod[OPT];
+        uint2 ro[OPT];
+        uint32_t obj[OPT], vis[OPT];
 #pragma unroll
         for (int k = 0; k < OPT; ++k) {
-            visPrev[k] = nvis[k];
-            // in range (LATE marks it in bit 31), and pass 1: visible last frame (drawOccFirst.cs.hlsl:22-25)
-            act[k] = visPrev[k] != 0u;
-            const uint2 ro = nro[k];
-            ok[k] = act[k] && ro.x < sc.transformCount && ro.y < sc.surfaceCount;
-            const uint32_t tid = ok[k] ? ro.x : 0u, sid = ok[k] ? ro.y : 0u;
-            const BlzMeshTransform* tt = sc.transforms;
-            if constexpr (!SINGLE) {
-                if (bv.dynT != nullptr && tid < bv.dynCount) tt = bv.dynT;
-            }
-            const float4* tp = reinterpret_cast<const float4*>(tt + tid);
-            const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + sid);
-            ps[k] = __ldg(tp);
-            q[k] = __ldg(tp + 1);
-            sph[k] = __ldg(sp);
-            const uint4 s1 = __ldg(reinterpret_cast<const uint4*>(sp + 1));  // materialId, lodOffset, lodCount, vertexOffset
-            lod[k] = make_uint2(s1.y, s1.z);
+            ro[k] = nro[k];
+            vis[k] = nvis[k];  // in range (LATE marks it in bit 31); pass 1: visible last frame (drawOccFirst.cs.hlsl:22-25)
+            obj[k] = sb + k * 32u + lane;
         }
-        if (sb + STEP < limit) prefetch(sb + STEP);
+        if constexpr (PACK) {
+            if (sb + STEP < limit) prefetch(sb + STEP);
 #pragma unroll
-        for (int k = 0; k < OPT; ++k) {
-            const bool lodOk = lod[k].x < sc.lodCount && lod[k].y <= sc.lodCount - lod[k].x;
-            const bool good = ok[k] && lodOk;
-            if (act[k] && !good) flags |= BLZ_FLAG_BAD_INDEX;
-            const Vec3 c = view_transform(v.rows, model_to_world(Vec3{sph[k].x, sph[k].y, sph[k].z}, ps[k], q[k]));
-            const float r = BLZ_FM(sph[k].w, ps[k].w);
-            const bool inFrustum = good && frustum_check(c, r, v);
-            const uint32_t i = sb + k * 32u + lane;
-            if (MODE == BLZ_MODE_LATE && act[k] && !inFrustum) bv.vis[i] = 0u;  // drawOccLate.cs.hlsl:67
-            const unsigned m = __ballot_sync(0xFFFFFFFFu, inFrustum);
-            if (inFrustum) {
-                uint4* e = reinterpret_cast<uint4*>(ring + ((tail + __popc(m & lanemask_lt())) & (kRing - 1u)));
-                const uint32_t tag = (MODE == BLZ_MODE_LATE && (visPrev[k] & 0x7FFFFFFFu) != 0u) ? 0x80000000u : 0u;
-                e[0] = make_uint4(i | tag, __float_as_uint(c.x), __float_as_uint(c.y), __float_as_uint(c.z));
-                e[1] = make_uint4(__float_as_uint(r), __float_as_uint(ps[k].w), lod[k].x, lod[k].y);
+            for (int k = 0; k < OPT; ++k) {
+                const bool act = vis[k] != 0u;
+                const unsigned m = __ballot_sync(0xFFFFFFFFu, act);
+                if (act) cand[(atail + __popc(m & lanemask_lt())) & (2u * STEP - 1u)] = make_uint4(obj[k], ro[k].x, ro[k].y, 0u);
+                atail += __popc(m);
             }
-            tail += __popc(m);
-            if (tail - head >= 32u) {
-                __syncwarp();
-                dense_round<MODE>(sc, bv, v, ring, head, 32u, stage, run);
-                head += 32u;
-                __syncwarp();
-            }
+            if (atail - ahead >= STEP) take_candidates(STEP);
+        } else {
+            gather(ro, vis);
+            if (sb + STEP < limit) prefetch(sb + STEP);
+            test(obj, vis);
         }
+    }
+    if constexpr (PACK) {
+        if (atail != ahead) take_candidates(atail - ahead);
     }
     if (tail != head) {
         __syncwarp();
@@ -223,6 +275,8 @@ template <int MODE, bool SINGLE, int THREADS, int OPT>
 __global__ void __launch_bounds__(THREADS, SINGLE ? 1024 / THREADS : 1) cull_decide_kernel(const PipeParams p) {
     constexpr int NW = THREADS / 32;
     __shared__ __align__(16) Survivor s_ring[NW][kRing];
+    constexpr bool PACK = (MODE == BLZ_MODE_FIRST) && SINGLE;
+    __shared__ uint4 s_cand[PACK ? NW : 1][PACK ? 2 * 32 * OPT : 1];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t warpsTotal = gridDim.x * NW;
     const uint32_t chunkSize = p.chunkSize;
@@ -249,16 +303,17 @@ __global__ void __launch_bounds__(THREADS, SINGLE ? 1024 / THREADS : 1) cull_dec
         const uint32_t limit = min(base + chunkSize, bv.count);
         uint2* stage = p.staged + static_cast<size_t>(chunk) * chunkSize;
         Survivor* ring = s_ring[warp];
+        uint4* cand = s_cand[PACK ? warp : 0];
         uint32_t total = 0;
         if (MODE == kModeRuntime) {
             switch (bv.mode) {
-                case BLZ_MODE_FIRST: total = decide_run_warp<BLZ_MODE_FIRST, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
-                case BLZ_MODE_LATE: total = decide_run_warp<BLZ_MODE_LATE, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
-                case BLZ_MODE_TEMPORAL: total = decide_run_warp<BLZ_MODE_TEMPORAL, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
-                default: total = decide_run_warp<BLZ_MODE_FRUSTUM, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, flags); break;
+                case BLZ_MODE_FIRST: total = decide_run_warp<BLZ_MODE_FIRST, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, flags); break;
+                case BLZ_MODE_LATE: total = decide_run_warp<BLZ_MODE_LATE, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, flags); break;
+                case BLZ_MODE_TEMPORAL: total = decide_run_warp<BLZ_MODE_TEMPORAL, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, flags); break;
+                default: total = decide_run_warp<BLZ_MODE_FRUSTUM, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, flags); break;
             }
         } else {
-            total = decide_run_warp<(MODE < 0 ? 0 : MODE), SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, flags);
+            total = decide_run_warp<(MODE < 0 ? 0 : MODE), SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, flags);
         }
         if (lane == 0) p.chunkCount[chunk] = total;
         chunk = next;
