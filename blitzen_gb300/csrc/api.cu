@@ -252,11 +252,12 @@ int blz_scene_upload(blz_ctx* c, const BlzSceneDesc* s, uint32_t flags, blz_stre
             return e == cudaErrorMemoryAllocation ? fail(BLZ_ERR_OUT_OF_MEMORY, "scene allocation failed") : cuda_fail(e, "scene upload");
         }
     }
-    if (reinterpret_cast<uintptr_t>(t.transforms) % 16 || reinterpret_cast<uintptr_t>(t.surfaces) % 16 ||
+    if (reinterpret_cast<uintptr_t>(t.transforms) % 32 || reinterpret_cast<uintptr_t>(t.surfaces) % 16 ||
         reinterpret_cast<uintptr_t>(t.lods) % 16 || reinterpret_cast<uintptr_t>(t.clusters) % 16 ||
         reinterpret_cast<uintptr_t>(t.objects) % 8) {
         release_scene(c);
-        return fail(BLZ_ERR_INVALID_ARGUMENT, "scene tables must be 16-byte aligned (render objects 8-byte)");
+        return fail(BLZ_ERR_INVALID_ARGUMENT,
+                    "scene tables must be aligned: transforms 32 bytes, surfaces/LODs/clusters 16, render objects 8");
     }
     c->scene = t;
     c->defaultObjects = t.objects;

@@ -36,8 +36,8 @@ static int build_views(blz_ctx* c, const BlzBatchView* views, uint32_t n, uint32
             if (rc != BLZ_OK) return rc;
         }
         if (v.dynamicCount && !v.dynamicTransforms) return fail(BLZ_ERR_INVALID_ARGUMENT, "view %u: dynamic transforms are NULL", i);
-        if (reinterpret_cast<uintptr_t>(v.dynamicTransforms) % 16)
-            return fail(BLZ_ERR_INVALID_ARGUMENT, "view %u: dynamic transforms must be 16-byte aligned", i);
+        if (reinterpret_cast<uintptr_t>(v.dynamicTransforms) % 32)
+            return fail(BLZ_ERR_INVALID_ARGUMENT, "view %u: dynamic transforms must be 32-byte aligned", i);
         BatchViewDev d{};
         d.view = v.view;
         d.objects = objs;

@@ -384,6 +384,15 @@ __device__ __forceinline__ uint32_t lookback_warp(unsigned long long* states, ui
     return resolve_prefix_warp(states, tile, firstTile, epoch, aggregate, status);
 }
 
+// One MeshTransform {pos.xyz, scale, quat.xyzw} in a single 256-bit read-only load (the table
+// is 32-byte aligned, checked on upload).
+__device__ __forceinline__ void ldg_transform(const BlzMeshTransform* t, float4& posScale, float4& q) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(posScale.x), "=f"(posScale.y), "=f"(posScale.z), "=f"(posScale.w), "=f"(q.x), "=f"(q.y), "=f"(q.z),
+          "=f"(q.w)
+        : "l"(t));
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

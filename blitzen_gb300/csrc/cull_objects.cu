@@ -100,6 +100,14 @@ __device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchVi
     run += __popc(e);
 }
 
+// The fields of the surface table the frustum stage reads (bounding sphere; LOD offset and count),
+// copied into shared memory by each block when the table is small enough; null pointers: read the
+// table in global memory.
+struct SurfaceCache {
+    const float4* sphere;
+    const uint2* lod;
+};
+
 // One warp decides the objects [base, limit) of a view, 32 * OPT at a time (object
 // sb + k * 32 + lane for k < OPT, so lanes ascend within each 32-object slice):
 //   1  every lane loads its OPT render objects (fetched one step ahead) and their transforms and
@@ -115,7 +123,7 @@ __device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchVi
 template <int MODE, bool SINGLE, int OPT>
 __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const BatchViewDev& bv, uint32_t base,
                                                     uint32_t limit, uint2* stage, Survivor* ring, uint4* cand,
-                                                    unsigned int& flags) {
+                                                    const SurfaceCache& surf, unsigned int& flags) {
     constexpr uint32_t STEP = 32u * OPT;
     constexpr bool PACK = (MODE == BLZ_MODE_FIRST) && SINGLE;  // candidate ring of 2 * STEP entries
     const uint32_t lane = threadIdx.x & 31u;
@@ -145,13 +153,16 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
             if constexpr (!SINGLE) {
                 if (bv.dynT != nullptr && tid < bv.dynCount) tt = bv.dynT;
             }
-            const float4* tp = reinterpret_cast<const float4*>(tt + tid);
-            const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + sid);
-            ps[k] = __ldg(tp);
-            q[k] = __ldg(tp + 1);
-            sph[k] = __ldg(sp);
-            const uint4 s1 = __ldg(reinterpret_cast<const uint4*>(sp + 1));  // materialId, lodOffset, lodCount, vertexOffset
-            lod[k] = make_uint2(s1.y, s1.z);
+            ldg_transform(tt + tid, ps[k], q[k]);
+            if (surf.sphere != nullptr) {
+                sph[k] = surf.sphere[sid];
+                lod[k] = surf.lod[sid];
+            } else {
+                const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + sid);
+                sph[k] = __ldg(sp);
+                const uint4 s1 = __ldg(reinterpret_cast<const uint4*>(sp + 1));  // materialId, lodOffset, lodCount, vertexOffset
+                lod[k] = make_uint2(s1.y, s1.z);
+            }
         }
     };
     auto test = [&](const uint32_t (&obj)[OPT], const uint32_t (&vis)[OPT]) {
@@ -277,6 +288,23 @@ __global__ void __launch_bounds__(THREADS, SINGLE ? 1024 / THREADS : 1) cull_dec
     __shared__ __align__(16) Survivor s_ring[NW][kRing];
     constexpr bool PACK = (MODE == BLZ_MODE_FIRST) && SINGLE;
     __shared__ uint4 s_cand[PACK ? NW : 1][PACK ? 2 * 32 * OPT : 1];
+    // the surface table in shared memory, in what static shared memory is left (48 KB per block)
+    constexpr size_t kUsed = sizeof(Survivor) * kRing * NW + (PACK ? sizeof(uint4) * NW * 2 * 32 * OPT : 0);
+    constexpr size_t kLeft = kUsed + 1024 < 48 * 1024 ? 48 * 1024 - 1024 - kUsed : 0;
+    constexpr uint32_t kSurf = kLeft >= 512 * 24 ? 512u : (kLeft >= 256 * 24 ? 256u : (kLeft >= 64 * 24 ? 64u : 1u));
+    __shared__ float4 s_sphere[kSurf];
+    __shared__ uint2 s_lod[kSurf];
+    SurfaceCache surf{nullptr, nullptr};
+    if (kSurf > 1u && p.sc.surfaceCount <= kSurf) {
+        for (uint32_t i = threadIdx.x; i < p.sc.surfaceCount; i += THREADS) {
+            const float4* sp = reinterpret_cast<const float4*>(p.sc.surfaces + i);
+            s_sphere[i] = __ldg(sp);
+            const uint4 s1 = __ldg(reinterpret_cast<const uint4*>(sp + 1));
+            s_lod[i] = make_uint2(s1.y, s1.z);
+        }
+        __syncthreads();
+        surf = SurfaceCache{s_sphere, s_lod};
+    }
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t warpsTotal = gridDim.x * NW;
     const uint32_t chunkSize = p.chunkSize;
@@ -307,13 +335,13 @@ __global__ void __launch_bounds__(THREADS, SINGLE ? 1024 / THREADS : 1) cull_dec
         uint32_t total = 0;
         if (MODE == kModeRuntime) {
             switch (bv.mode) {
-                case BLZ_MODE_FIRST: total = decide_run_warp<BLZ_MODE_FIRST, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, flags); break;
-                case BLZ_MODE_LATE: total = decide_run_warp<BLZ_MODE_LATE, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, flags); break;
-                case BLZ_MODE_TEMPORAL: total = decide_run_warp<BLZ_MODE_TEMPORAL, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, flags); break;
-                default: total = decide_run_warp<BLZ_MODE_FRUSTUM, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, flags); break;
+                case BLZ_MODE_FIRST: total = decide_run_warp<BLZ_MODE_FIRST, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags); break;
+                case BLZ_MODE_LATE: total = decide_run_warp<BLZ_MODE_LATE, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags); break;
+                case BLZ_MODE_TEMPORAL: total = decide_run_warp<BLZ_MODE_TEMPORAL, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags); break;
+                default: total = decide_run_warp<BLZ_MODE_FRUSTUM, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags); break;
             }
         } else {
-            total = decide_run_warp<(MODE < 0 ? 0 : MODE), SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, flags);
+            total = decide_run_warp<(MODE < 0 ? 0 : MODE), SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags);
         }
         if (lane == 0) p.chunkCount[chunk] = total;
         chunk = next;

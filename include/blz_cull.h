@@ -114,7 +114,9 @@ typedef struct BlzSceneDesc {
 
 /* Makes a scene resident: render objects, transforms, surfaces, LODs, clusters in the reference
  * layouts. Replaces StaticBuffersInit / SetupForRendering
- * (src/Renderer/BlitzenVulkan/vulkanRendererSetup.cpp:453-522, dx12Renderer.h:22-43). */
+ * (src/Renderer/BlitzenVulkan/vulkanRendererSetup.cpp:453-522, dx12Renderer.h:22-43).
+ * Borrowed device tables must be aligned: transforms to 32 bytes (one transform is read in a
+ * single 32-byte load), surfaces, LODs and clusters to 16, render objects to 8. */
 int blz_scene_upload(blz_ctx* ctx, const BlzSceneDesc* scene, uint32_t flags, blz_stream_t stream);
 
 /* Device pointers of the resident tables (for callers that build render lists on the device). */
@@ -260,7 +262,7 @@ typedef struct BlzBatchView {
     uint32_t* visibility;            /* device; FIRST and LATE */
     const BlzPyramid* pyramid;       /* host descriptor; LATE and TEMPORAL */
     BlzCullTarget target;
-    const BlzMeshTransform* dynamicTransforms; /* device; overrides transforms[0, dynamicCount) */
+    const BlzMeshTransform* dynamicTransforms; /* device, 32-byte aligned; overrides transforms[0, dynamicCount) */
     uint32_t dynamicCount;
     uint32_t reserved1;
 } BlzBatchView;
