@@ -11,9 +11,10 @@ restored to the 50% mask and L2 is flushed (a 512 MiB read), both outside the ti
 value  = objects per second of the device-timed frames: each step replays the frame (the three passes,
          recorded once with blz_capture_begin/end) as one CUDA graph between two CUDA events; the
          per-pass breakdown in `roofline` replays each pass as its own graph.
-e2e    = the same frame through the C ABI with host buffers: per step the depth buffer (8.3 MB) and
-         the 1,000 dynamic transforms are copied from pinned host memory and both draw counts are
-         read back, all inside the timed region.
+e2e    = the same frame through the C ABI with host buffers: per step the 1,000 dynamic transforms
+         (blz_transforms_update) and the depth buffer (8.3 MB) are copied from pinned host memory,
+         the recorded frame is replayed (blz_graph_launch) and both draw counts are read back, all
+         inside the timed region; `direct_calls` is the same with the three passes called directly.
 --impl reference runs the CPU oracle (a port of the reference's shaders, all host threads) on the
 same frames.
 """
@@ -337,30 +338,40 @@ def main():
     dyn_ids = np.arange(DYNAMIC, dtype=np.uint32)
     dyn_tr = sc.transforms[:DYNAMIC].copy()
     hcounts = torch.empty(2, dtype=torch.int32, pin_memory=True)
-    e2e_ms = []
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for k in range(args.warmup + args.steps):
-        vis.copy_(vis0)
-        flush_l2()
-        dyn_tr["orientation"] = S.random_unit_quaternions(rng, DYNAMIC)
-        torch.cuda.synchronize()
-        e0.record()
-        c.update_object_transform(dyn_ids, dyn_tr)
-        depth.copy_(hdepth, non_blocking=True)
-        step_direct()  # the C-ABI calls themselves, host issue included
-        hcounts[0:1].copy_(t1.count, non_blocking=True)
-        hcounts[1:2].copy_(t2.count, non_blocking=True)
-        e1.record()
-        e1.synchronize()
-        if k >= args.warmup:
-            e2e_ms.append(e0.elapsed_time(e1))
-    t_e2e = sum(e2e_ms) / len(e2e_ms)
-    if world > 1:
-        tt = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+
+    def e2e_run(frame_call):
+        out = []
+        for k in range(args.warmup + args.steps):
+            vis.copy_(vis0)
+            flush_l2()
+            dyn_tr["orientation"] = S.random_unit_quaternions(rng, DYNAMIC)
+            torch.cuda.synchronize()
+            e0.record()
+            c.update_object_transform(dyn_ids, dyn_tr)  # blz_transforms_update: host rows via pinned staging
+            depth.copy_(hdepth, non_blocking=True)
+            frame_call()
+            hcounts[0:1].copy_(t1.count, non_blocking=True)
+            hcounts[1:2].copy_(t2.count, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            if k >= args.warmup:
+                out.append(e0.elapsed_time(e1))
+        t = sum(out) / len(out)
+        if world > 1:
+            tt = torch.tensor([t], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t = float(tt.item())
+        return t
+
+    # the frame as a user replays it (blz_graph_launch of the recorded frame), and as direct calls
+    t_e2e = e2e_run(frame.launch)
+    t_e2e_direct = e2e_run(step_direct)
     e2e = {"value": N * world / (t_e2e * 1e-3), "unit": "objects/s", "ms_per_step": t_e2e,
-           "h2d_bytes_per_step": W * H * 4 + DYNAMIC * (32 + 4), "d2h_bytes_per_step": 8}
+           "h2d_bytes_per_step": W * H * 4 + DYNAMIC * (32 + 4), "d2h_bytes_per_step": 8,
+           "path": "blz_transforms_update + depth H2D + blz_graph_launch(recorded frame) + count D2H",
+           "direct_calls": {"value": N * world / (t_e2e_direct * 1e-3), "ms_per_step": t_e2e_direct,
+                            "path": "same, with blz_cull_first / blz_pyramid_build / blz_cull_late called directly"}}
 
     extras = {}
     if not args.no_extras and rank == 0:
