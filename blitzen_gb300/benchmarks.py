@@ -9,6 +9,8 @@ batched_views  64 views over the resident stress scene, each with its own camera
 serving        the request loop over the resident scene: Poisson arrivals at 2,000 requests/s, each a
                camera over a window of 1k..1M objects with the 1,000 dynamic objects rotated by
                0.01 rad about random axes; p50/p99 latency from arrival to result and objects/s.
+instanced      the instanced cull over the resident scene (256 LODs x 100k instance slots).
+clusters       the cluster cull over 50k objects of ~200 clusters each, with Hi-Z and cone test.
 """
 from __future__ import annotations
 
@@ -201,8 +203,92 @@ def serving(culler, scene, device, seconds=3.0, rate=2000.0, seed=0) -> dict:
             "objects_per_s": float(counts.sum()) / elapsed, "errors": int(sum(1 for s in released if s))}
 
 
+def _replay_ms(culler, fn, reps, flush, stream) -> float:
+    """Median CUDA-event time of `fn` recorded once and replayed as a graph, L2 flushed before each."""
+    with torch.cuda.stream(stream):
+        fn()
+        culler.capture_begin()
+        fn()
+        g = culler.capture_end()
+        for _ in range(3):
+            g.launch()
+        times = []
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(reps):
+            flush.sum(dtype=torch.int64)
+            a.record()
+            g.launch()
+            b.record()
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        g.close()
+    return float(np.median(times))
+
+
+def instanced(culler, scene, device, reps=30, slots=100_000) -> dict:
+    """The instanced cull (drawInstCull) over the resident stress scene, 256 LODs x 100k slots."""
+    v = abi.view_setup(S.fov_radians(), float(W), float(H), S.ZNEAR, 1e4, (0, 0, 0), 0, 0, W / 2, H / 2)
+    n_lods = len(scene.lods)
+    ctr = np.zeros(n_lods, abi.LOD_INSTANCE_COUNTER)
+    ctr["instanceOffset"] = np.arange(n_lods, dtype=np.uint64) * slots
+    dctr = to_device(ctr, device)
+    inst = torch.empty(n_lods * slots, dtype=torch.int32, device=device)
+    t = Target.alloc(n_lods, abi.STRIDE_VULKAN, device)
+    flush = torch.ones(128 << 20, dtype=torch.int32, device=device)
+    side = torch.cuda.Stream(device)
+    ms = _replay_ms(culler, lambda: culler.draw_instance_cull_pass(v, dctr, inst, slots, t), reps, flush, side)
+    culler.check(side)
+    counts = dctr.cpu().numpy().view(np.uint32).reshape(-1, 2)[:, 1]
+    visible = int(counts.sum())
+    n_cmd = int(t.read()[0])
+    nbytes = scene.count * (8 + 32) + 4 * visible + 8 * n_lods * 2 + n_cmd * abi.STRIDE_VULKAN
+    return {"objects": scene.count, "visible_instances": visible, "commands": n_cmd, "ms": ms,
+            "objects_per_s": scene.count / (ms * 1e-3), "algorithmic_bytes": nbytes,
+            "GB/s": nbytes / (ms * 1e-3) / 1e9}
+
+
+def clusters(device, reps=30) -> dict:
+    """The cluster cull over the cluster configuration: 50k objects, 32 meshes of ~200 clusters,
+    frustum + Hi-Z + LOD per object, then sphere frustum + Hi-Z + normal cone per cluster."""
+    from .culler import Culler
+    sc = S.cluster_scene(50_000, seed=0)
+    c = Culler(device.index if device.index is not None else 0)
+    try:
+        c.setup_for_rendering(sc)
+        v = abi.view_setup(S.fov_radians(), float(W), float(H), S.ZNEAR, 1e4, (0.0, 0.0, -50.0), 0, 0, W / 2, H / 2)
+        depth = torch.zeros(W * H, dtype=torch.float32, device=device)
+        c.raster_boxes(v, torch.from_numpy(sc.boxes.reshape(-1)).to(device), depth, W, H)
+        pyr = DevicePyramid(W, H, abi.HIZ_D3D12, device)
+        c.generate_depth_pyramid(pyr, depth)
+        per_surface = np.array([int(sc.lods[int(s["lodOffset"]):int(s["lodOffset"]) + int(s["lodCount"])]["clusterCount"].max())
+                                for s in sc.surfaces], np.int64)
+        cap = int(per_surface[sc.objects["surfaceId"]].sum())
+        t = Target.alloc(cap, abi.STRIDE_VULKAN, device)
+        ids = torch.empty(cap, dtype=torch.int32, device=device)
+        flush = torch.ones(128 << 20, dtype=torch.int32, device=device)
+        side = torch.cuda.Stream(device)
+        ms = _replay_ms(c, lambda: c.cluster_cull(v, t, pyramid=pyr, cluster_ids=ids), reps, flush, side)
+        c.check(side)
+        n = int(t.read()[0])
+        nbytes = sc.count * (8 + 32) + sc.clusters.nbytes + n * (abi.STRIDE_VULKAN + 4)
+        return {"objects": sc.count, "clusters_in_scene": len(sc.clusters), "cluster_upper_bound": cap,
+                "clusters_emitted": n, "ms": ms, "objects_per_s": sc.count / (ms * 1e-3),
+                "cluster_candidates_per_s": cap / (ms * 1e-3), "algorithmic_bytes": nbytes,
+                "GB/s": nbytes / (ms * 1e-3) / 1e9}
+    finally:
+        c.close()
+
+
 def run_extras(culler, scene, device) -> dict:
     out = {}
+    try:
+        out["instanced"] = instanced(culler, scene, device)
+    except Exception as ex:
+        out["instanced"] = {"error": repr(ex)}
+    try:
+        out["clusters"] = clusters(device)
+    except Exception as ex:
+        out["clusters"] = {"error": repr(ex)}
     try:
         out["batched_views"] = batched_views(culler, scene, device)
     except Exception as ex:
