@@ -13,10 +13,10 @@ value  = objects per second of the device-timed frames: each step replays the fr
          per-pass breakdown in `roofline` replays each pass as its own graph.
 e2e    = the same frame through the C ABI with host buffers: per step the 1,000 dynamic transforms
          (blz_transforms_update) and the depth buffer (8.3 MB) are copied from pinned host memory,
-         the recorded passes are replayed (blz_graph_launch; the depth upload runs on a second
-         stream beside pass 1, which does not read it) and both draw counts are read back, all
-         inside the timed region; `serial_upload` and `direct_calls` are the same without the
-         overlap and with the three passes called directly.
+         the recorded frame is replayed (blz_graph_launch) and both draw counts are read back, all
+         inside the timed region; `direct_calls` is the same with the three passes called directly.
+         (Uploading the depth on a second stream beside pass 1 measured slower: both compete for
+         the same DRAM bandwidth.)
 --impl reference runs the CPU oracle (a port of the reference's shaders, all host threads) on the
 same frames.
 """
@@ -342,18 +342,7 @@ def main():
     hcounts = torch.empty(2, dtype=torch.int32, pin_memory=True)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
-    copy_stream = torch.cuda.Stream(dev)
-    copied = torch.cuda.Event()
-
-    def overlapped_frame():
-        # the depth upload runs on its own stream beside pass 1, which does not read it; the
-        # pyramid and pass 2 wait for it
-        passes[0].launch()
-        torch.cuda.current_stream(dev).wait_event(copied)
-        passes[1].launch()
-        passes[2].launch()
-
-    def e2e_run(frame_call, overlap=False):
+    def e2e_run(frame_call):
         out = []
         for k in range(args.warmup + args.steps):
             vis.copy_(vis0)
@@ -361,14 +350,8 @@ def main():
             dyn_tr["orientation"] = S.random_unit_quaternions(rng, DYNAMIC)
             torch.cuda.synchronize()
             e0.record()
-            if overlap:
-                copy_stream.wait_event(e0)
-                with torch.cuda.stream(copy_stream):
-                    depth.copy_(hdepth, non_blocking=True)
-                    copied.record()
             c.update_object_transform(dyn_ids, dyn_tr)  # blz_transforms_update: host rows via pinned staging
-            if not overlap:
-                depth.copy_(hdepth, non_blocking=True)
+            depth.copy_(hdepth, non_blocking=True)
             frame_call()
             hcounts[0:1].copy_(t1.count, non_blocking=True)
             hcounts[1:2].copy_(t2.count, non_blocking=True)
@@ -383,19 +366,14 @@ def main():
             t = float(tt.item())
         return t
 
-    # the frame as a user replays it (recorded passes through blz_graph_launch, the depth upload
-    # overlapped with pass 1), as one recorded frame after the upload, and as direct calls
-    t_e2e = e2e_run(overlapped_frame, overlap=True)
-    t_e2e_serial = e2e_run(frame.launch)
+    # the frame as a user replays it (the recorded frame through blz_graph_launch), and as direct calls
+    t_e2e = e2e_run(frame.launch)
     t_e2e_direct = e2e_run(step_direct)
     e2e = {"value": N * world / (t_e2e * 1e-3), "unit": "objects/s", "ms_per_step": t_e2e,
            "h2d_bytes_per_step": W * H * 4 + DYNAMIC * (32 + 4), "d2h_bytes_per_step": 8,
-           "path": "blz_transforms_update; depth H2D on a second stream beside pass 1 (blz_graph_launch); "
-                   "pyramid + pass 2 (blz_graph_launch); count D2H",
-           "serial_upload": {"value": N * world / (t_e2e_serial * 1e-3), "ms_per_step": t_e2e_serial,
-                             "path": "blz_transforms_update + depth H2D, then the recorded frame"},
+           "path": "blz_transforms_update + depth H2D + blz_graph_launch(recorded frame) + count D2H",
            "direct_calls": {"value": N * world / (t_e2e_direct * 1e-3), "ms_per_step": t_e2e_direct,
-                            "path": "serial upload, with blz_cull_first / blz_pyramid_build / blz_cull_late called directly"}}
+                            "path": "same, with blz_cull_first / blz_pyramid_build / blz_cull_late called directly"}}
 
     extras = {}
     if not args.no_extras and rank == 0:

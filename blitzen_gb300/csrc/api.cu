@@ -176,6 +176,7 @@ int blz_ctx_destroy(blz_ctx* c) {
     if (c->batchDev) cudaFree(c->batchDev);
     if (c->stagingDev) cudaFree(c->stagingDev);
     if (c->chunkMem) cudaFree(c->chunkMem);
+    if (c->instScratch) cudaFree(c->instScratch);
     delete c;
     return BLZ_OK;
 }
@@ -496,6 +497,63 @@ int blz_cull_instanced(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList 
     const uint32_t nL = c->scene.lodCount;
     if (nL == 0) return fail(BLZ_ERR_INVALID_ARGUMENT, "the scene has no LODs");
     if (nL > kMaxInstancedLods) return fail(BLZ_ERR_INVALID_ARGUMENT, "instanced cull supports up to %u LODs, scene has %u", kMaxInstancedLods, nL);
+    if (nL <= kInstStagedMaxLods) {
+        // the FRUSTUM decide kernel stages (object, LOD) pairs; a counting sort turns them into lists
+        const uint32_t tile = single_chunk_size(BLZ_MODE_FRUSTUM, c->singleThreads, c->singleOpt, count, c->smCount);
+        uint32_t chunks = (count + tile - 1) / tile;
+        if (chunks == 0) chunks = 1;
+        rc = ensure_chunk_scratch(c, chunks, tile);
+        if (rc != BLZ_OK) return rc;
+        const uint32_t groups = instanced_group_count(chunks);
+        const size_t words = static_cast<size_t>(groups) * nL + nL;
+        if (words > c->instWords) {
+            if (c->capturing) return fail(BLZ_ERR_CAPACITY, "scratch must grow, which a capture cannot record: run the call once before capturing");
+            if (c->instScratch) {
+                cudaDeviceSynchronize();
+                cudaFree(c->instScratch);
+                c->instScratch = nullptr;
+                c->instWords = 0;
+            }
+            const size_t want = words + words / 4;
+            if (cudaMalloc(&c->instScratch, want * sizeof(uint32_t)) != cudaSuccess)
+                return fail(BLZ_ERR_OUT_OF_MEMORY, "instanced scratch of %zu bytes", want * sizeof(uint32_t));
+            c->instWords = want;
+        }
+        PipeParams p{};
+        p.sc = c->scene;
+        p.single.view = *view;
+        p.single.objects = objs;
+        p.single.count = count;
+        p.single.mode = BLZ_MODE_FRUSTUM;
+        p.viewCount = 1;
+        p.totalTiles = chunks;
+        p.chunkSize = tile;
+        bind_chunk_scratch(c, p);
+        p.workCounter = nullptr;
+        InstStagedParams q{};
+        q.staged = p.staged;
+        q.chunkCount = p.chunkCount;
+        q.totalTiles = chunks;
+        q.chunkSize = tile;
+        q.groups = groups;
+        q.nL = nL;
+        q.hist = c->instScratch;
+        q.totals = c->instScratch + static_cast<size_t>(groups) * nL;
+        q.lods = c->scene.lods;
+        q.counters = counters;
+        q.instances = instances;
+        q.instanceCapacity = instanceCapacity;
+        q.slotsPerLod = slotsPerLod;
+        q.cmds = static_cast<uint8_t*>(target->commands);
+        q.stride = target->stride;
+        q.capacity = target->capacity;
+        q.drawCount = target->drawCount;
+        q.status = &c->scratch->status;
+        cudaError_t e = launch_instanced_staged(p, q, c->singleThreads, c->singleOpt, c->smCount, reinterpret_cast<cudaStream_t>(s));
+        if (e != cudaSuccess) return cuda_fail(e, "instanced cull launch");
+        c->launches += 4;  // decide, count, offsets, place
+        return BLZ_OK;
+    }
     const uint32_t tiles = (count + instanced_tile_size() - 1) / instanced_tile_size();
     rc = ensure_states(c, (size_t)(tiles ? tiles : 1) * nL);
     if (rc != BLZ_OK) return rc;

@@ -34,6 +34,8 @@ struct blz_ctx {
     void* chunkMem = nullptr;          // object-cull staging: records, chunk counts
     size_t chunkObjects = 0;           // staged-record capacity
     size_t chunkSlots = 0;             // chunk count capacity
+    uint32_t* instScratch = nullptr;   // instanced cull: group x LOD counts, then LOD totals
+    size_t instWords = 0;
     bool hasScene = false;
     blz::SceneT scene{};
     const BlzRenderObject* defaultObjects = nullptr;

@@ -456,7 +456,7 @@ static uint32_t occupancy_t() {
 }
 
 template <int MODE, bool SINGLE, int THREADS, int OPT>
-static cudaError_t launch_t(const PipeParams& p, uint32_t blocksPerSm, int smCount, cudaStream_t s) {
+static cudaError_t launch_decide_t(const PipeParams& p, uint32_t blocksPerSm, int smCount, cudaStream_t s) {
     auto kern = cull_decide_kernel<MODE, SINGLE, THREADS, OPT>;
     const uint32_t occ = occupancy_t<MODE, SINGLE, THREADS, OPT>();
     const uint32_t per = blocksPerSm ? (blocksPerSm < occ ? blocksPerSm : occ) : occ;
@@ -465,7 +465,12 @@ static cudaError_t launch_t(const PipeParams& p, uint32_t blocksPerSm, int smCou
     if (grid > needed) grid = needed;
     if (grid == 0) grid = 1;
     kern<<<grid, THREADS, 0, s>>>(p);
-    cudaError_t e = cudaGetLastError();
+    return cudaGetLastError();
+}
+
+template <int MODE, bool SINGLE, int THREADS, int OPT>
+static cudaError_t launch_t(const PipeParams& p, uint32_t blocksPerSm, int smCount, cudaStream_t s) {
+    cudaError_t e = launch_decide_t<MODE, SINGLE, THREADS, OPT>(p, blocksPerSm, smCount, s);
     if (e != cudaSuccess) return e;
     const uint32_t sgrid = (p.totalTiles + kScatterChunks - 1) / kScatterChunks;
     cull_scatter_kernel<SINGLE><<<sgrid ? sgrid : 1u, kScatterWarps * 32, 0, s>>>(p);
@@ -527,6 +532,186 @@ cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t thre
         case BLZ_MODE_TEMPORAL: return launch_single_mode<BLZ_MODE_TEMPORAL>(p, threads, opt, smCount, s);
         default: return cudaErrorInvalidValue;
     }
+}
+
+// ------------------------------------------------------------------ instanced cull from the staged records
+//
+// The instanced cull (drawInstCountReset + drawInstCull + drawInstCmd) decides exactly what the
+// frustum + LOD pass decides: every visible object and its LOD. So it runs the FRUSTUM decide
+// kernel, whose staged (objectId, lodId) records are in object order per chunk, and then turns
+// them into per-LOD instance lists with a stable counting sort over groups of kInstGroup chunks:
+//   count    per group, the number of records of each LOD (shared-memory histogram);
+//   offsets  per LOD, an exclusive scan of the group counts (one warp per LOD) and the total;
+//   place    per group, each warp counts its chunk's records per LOD, the block scans those rows
+//            per LOD, and each warp places its records in order (ranks inside 32-record slices
+//            from __match_any_sync); block 0 writes the counters and, in ascending LOD order, one
+//            command per non-empty LOD.
+
+constexpr uint32_t kInstGroup = 32;  // chunks per group, one warp each
+
+__global__ void __launch_bounds__(kInstGroup * 32) inst_count_kernel(const InstStagedParams q) {
+    extern __shared__ uint32_t s_hist[];  // [nL]
+    const uint32_t nL = q.nL;
+    for (uint32_t b = threadIdx.x; b < nL; b += kInstGroup * 32) s_hist[b] = 0u;
+    __syncthreads();
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t chunk = blockIdx.x * kInstGroup + warp;
+    if (chunk < q.totalTiles) {
+        const uint32_t n = __ldcg(q.chunkCount + chunk);
+        const uint2* st = q.staged + static_cast<size_t>(chunk) * q.chunkSize;
+        for (uint32_t j = lane; j < n; j += 32) atomicAdd(&s_hist[__ldcg(st + j).y], 1u);
+    }
+    __syncthreads();
+    uint32_t* h = q.hist + static_cast<size_t>(blockIdx.x) * nL;
+    for (uint32_t b = threadIdx.x; b < nL; b += kInstGroup * 32) h[b] = s_hist[b];
+}
+
+__global__ void __launch_bounds__(1024) inst_offsets_kernel(const InstStagedParams q) {
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t b = blockIdx.x * 32u + warp;
+    if (b >= q.nL) return;
+    uint32_t run = 0;
+    for (uint32_t g0 = 0; g0 < q.groups; g0 += 32u) {
+        const uint32_t g = g0 + lane;
+        const uint32_t x = g < q.groups ? __ldcg(q.hist + static_cast<size_t>(g) * q.nL + b) : 0u;
+        uint32_t incl = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= static_cast<uint32_t>(o)) incl += n;
+        }
+        if (g < q.groups) q.hist[static_cast<size_t>(g) * q.nL + b] = run + incl - x;
+        run += __shfl_sync(0xFFFFFFFFu, incl, 31);
+    }
+    if (lane == 0) q.totals[b] = run;
+}
+
+__global__ void __launch_bounds__(kInstGroup * 32) inst_place_kernel(const InstStagedParams q) {
+    extern __shared__ uint32_t s_rows[];  // [kInstGroup][nL]: per-warp counts, then offsets
+    __shared__ uint32_t s_warpSums[kInstGroup];
+    __shared__ unsigned int s_flags;
+    const uint32_t nL = q.nL;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    for (uint32_t j = threadIdx.x; j < kInstGroup * nL; j += kInstGroup * 32) s_rows[j] = 0u;
+    if (threadIdx.x == 0) s_flags = 0u;
+    __syncthreads();
+    const uint32_t chunk = blockIdx.x * kInstGroup + warp;
+    const bool have = chunk < q.totalTiles;
+    const uint32_t n = have ? __ldcg(q.chunkCount + chunk) : 0u;
+    const uint2* st = q.staged + static_cast<size_t>(chunk) * q.chunkSize;
+    uint32_t* row = s_rows + warp * nL;
+    const uint32_t lt = lanemask_lt();
+    // 1. this chunk's records per LOD (only this warp touches its row)
+    for (uint32_t j0 = 0; j0 < n; j0 += 32u) {
+        const uint32_t j = j0 + lane;
+        const uint32_t b = j < n ? __ldcg(st + j).y : 0xFFFFFFFFu;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
+        if (b != 0xFFFFFFFFu && (peers & lt) == 0u) row[b] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // 2. per LOD, exclusive offsets of the warps' chunks inside the group
+    for (uint32_t b = threadIdx.x; b < nL; b += kInstGroup * 32) {
+        uint32_t run = 0;
+        for (uint32_t w = 0; w < kInstGroup; ++w) {
+            const uint32_t c = s_rows[w * nL + b];
+            s_rows[w * nL + b] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    // 3. place the records in object order
+    const uint32_t* groupBase = q.hist + static_cast<size_t>(blockIdx.x) * nL;
+    const uint32_t slots = q.slotsPerLod ? q.slotsPerLod : 0xFFFFFFFFu;
+    unsigned int flags = 0u;
+    for (uint32_t j0 = 0; j0 < n; j0 += 32u) {
+        const uint32_t j = j0 + lane;
+        const uint2 rec = j < n ? __ldcg(st + j) : make_uint2(0u, 0xFFFFFFFFu);
+        const uint32_t b = rec.y;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
+        uint32_t before = 0;
+        if (b != 0xFFFFFFFFu) before = row[b];
+        __syncwarp();
+        if (b != 0xFFFFFFFFu) {
+            if ((peers & lt) == 0u) row[b] = before + __popc(peers);
+            const uint32_t pos = __ldcg(groupBase + b) + before + __popc(peers & lt);
+            const uint64_t at = static_cast<uint64_t>(__ldg(&q.counters[b].instanceOffset)) + pos;
+            if (pos < slots && at < q.instanceCapacity) q.instances[at] = rec.x;
+            else flags |= BLZ_FLAG_INSTANCE_OVERFLOW;
+        }
+        __syncwarp();
+    }
+    if (flags) atomicOr(&s_flags, flags);
+    // 4. block 0: counters and one command per non-empty LOD, in ascending LOD order
+    if (blockIdx.x == 0) {
+        const uint32_t per = (nL + kInstGroup * 32 - 1) / (kInstGroup * 32);
+        const uint32_t b0 = min(nL, threadIdx.x * per), b1 = min(nL, b0 + per);
+        uint32_t mine = 0;
+        for (uint32_t b = b0; b < b1; ++b) mine += __ldcg(q.totals + b) ? 1u : 0u;
+        uint32_t incl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= static_cast<uint32_t>(o)) incl += x;
+        }
+        if (lane == 31) s_warpSums[warp] = incl;
+        __syncthreads();
+        uint32_t warpOff = 0, all = 0;
+        for (uint32_t w = 0; w < kInstGroup; ++w) {
+            if (w < warp) warpOff += s_warpSums[w];
+            all += s_warpSums[w];
+        }
+        uint32_t out = warpOff + incl - mine;
+        unsigned int f = 0u;
+        for (uint32_t b = b0; b < b1; ++b) {
+            const uint32_t total = __ldcg(q.totals + b);
+            q.counters[b].instanceCount = total;
+            const uint32_t offset = __ldg(&q.counters[b].instanceOffset);
+            if (total > slots || static_cast<uint64_t>(offset) + min(total, slots) > q.instanceCapacity)
+                f |= BLZ_FLAG_INSTANCE_OVERFLOW;
+            if (total == 0u) continue;
+            if (out < q.capacity) {
+                uint32_t* w = reinterpret_cast<uint32_t*>(q.cmds + static_cast<size_t>(out) * q.stride);
+                const uint2 lod = __ldg(reinterpret_cast<const uint2*>(q.lods + b));  // indexCount, firstIndex
+                w[0] = offset;
+                w[1] = lod.x;
+                w[2] = min(total, slots);
+                w[3] = lod.y;
+                w[4] = 0u;
+                w[5] = 0u;
+            }
+            ++out;
+        }
+        if (all > q.capacity) f |= BLZ_FLAG_COMMAND_OVERFLOW;
+        if (f) atomicOr(&s_flags, f);
+        if (threadIdx.x == 0) *q.drawCount = all;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_flags) atomicOr(q.status, s_flags);
+}
+
+uint32_t instanced_group_count(uint32_t chunks) { return (chunks + kInstGroup - 1) / kInstGroup; }
+
+cudaError_t launch_instanced_staged(const PipeParams& p, const InstStagedParams& q, uint32_t threads, uint32_t opt,
+                                    int smCount, cudaStream_t s) {
+    cudaError_t e;
+    if (threads == 256 && opt == 1) e = launch_decide_t<BLZ_MODE_FRUSTUM, true, 256, 1>(p, 0, smCount, s);
+    else if (threads == 256 && opt == 4) e = launch_decide_t<BLZ_MODE_FRUSTUM, true, 256, 4>(p, 0, smCount, s);
+    else if (threads == 128 && opt == 2) e = launch_decide_t<BLZ_MODE_FRUSTUM, true, 128, 2>(p, 0, smCount, s);
+    else if (threads == 128 && opt == 4) e = launch_decide_t<BLZ_MODE_FRUSTUM, true, 128, 4>(p, 0, smCount, s);
+    else if (threads == 512 && opt == 1) e = launch_decide_t<BLZ_MODE_FRUSTUM, true, 512, 1>(p, 0, smCount, s);
+    else e = launch_decide_t<BLZ_MODE_FRUSTUM, true, kObjThreads, kObjOpt>(p, 0, smCount, s);
+    if (e != cudaSuccess) return e;
+    const size_t histBytes = sizeof(uint32_t) * q.nL;
+    const size_t rowBytes = sizeof(uint32_t) * kInstGroup * q.nL;
+    if (rowBytes > 48 * 1024) {
+        e = cudaFuncSetAttribute(inst_place_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(rowBytes));
+        if (e != cudaSuccess) return e;
+    }
+    inst_count_kernel<<<q.groups, kInstGroup * 32, histBytes, s>>>(q);
+    inst_offsets_kernel<<<(q.nL + 31) / 32, 1024, 0, s>>>(q);
+    inst_place_kernel<<<q.groups, kInstGroup * 32, rowBytes, s>>>(q);
+    return cudaGetLastError();
 }
 
 bool batch_shape_supported(uint32_t threads, uint32_t opt) {

@@ -107,6 +107,24 @@ struct InstancedParams {
     Scratch* scratch;
 };
 
+// The instanced cull's stages after the FRUSTUM decide kernel (see cull_objects.cu).
+struct InstStagedParams {
+    const uint2* staged;        // decide kernel output: [totalTiles * chunkSize] (objectId, lodId)
+    const uint32_t* chunkCount; // [totalTiles]
+    uint32_t totalTiles, chunkSize;
+    uint32_t groups, nL;        // chunk groups of the counting sort, LOD count
+    uint32_t* hist;             // scratch [groups * nL]: group counts, then exclusive offsets
+    uint32_t* totals;           // scratch [nL]
+    const BlzLodData* lods;
+    BlzLodInstanceCounter* counters;
+    uint32_t* instances;
+    uint32_t instanceCapacity, slotsPerLod;
+    uint8_t* cmds;
+    uint32_t stride, capacity;
+    uint32_t* drawCount;
+    unsigned int* status;
+};
+
 struct ClusterParams {
     SceneT sc;
     const BlzRenderObject* objects;
@@ -143,6 +161,10 @@ bool batch_shape_supported(uint32_t threads, uint32_t opt);
 cudaError_t launch_batch_cull(const PipeParams& p, uint32_t threads, uint32_t opt, uint32_t blocksPerSm, int smCount,
                               cudaStream_t s);
 uint32_t instanced_tile_size();
+constexpr uint32_t kInstStagedMaxLods = 1024;  // the staged instanced path keeps [32][LODs] counts in shared memory
+uint32_t instanced_group_count(uint32_t chunks);
+cudaError_t launch_instanced_staged(const PipeParams& p, const InstStagedParams& q, uint32_t threads, uint32_t opt,
+                                    int smCount, cudaStream_t s);
 cudaError_t launch_instanced_cull(const InstancedParams& p, const BlzCameraViewData& view, cudaStream_t s);
 uint32_t cluster_tile_objects();
 cudaError_t launch_cluster_cull(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s);
