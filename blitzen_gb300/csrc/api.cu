@@ -588,8 +588,9 @@ int blz_cull_clusters(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList l
     rc = check_pyramid(pyr, false);
     if (rc != BLZ_OK) return rc;
     if (!c->scene.clusters && c->scene.clusterCount) return fail(BLZ_ERR_INVALID_ARGUMENT, "scene has no cluster table");
-    const uint32_t tiles = (count + cluster_tile_objects() - 1) / cluster_tile_objects();
-    rc = ensure_states(c, tiles);
+    uint32_t tiles = (count + cluster_tile_objects() - 1) / cluster_tile_objects();
+    if (tiles == 0) tiles = 1;
+    rc = ensure_chunk_scratch(c, tiles, 1);  // one count per tile
     if (rc != BLZ_OK) return rc;
     ClusterParams p{};
     p.sc = c->scene;
@@ -603,9 +604,14 @@ int blz_cull_clusters(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList l
     p.clusterIds = clusterIds;
     p.drawCount = target->drawCount;
     p.scratch = c->scratch;
+    {
+        PipeParams scratch{};
+        bind_chunk_scratch(c, scratch);
+        p.tileCount = scratch.chunkCount;
+    }
     cudaError_t e = launch_cluster_cull(p, *view, reinterpret_cast<cudaStream_t>(s));
     if (e != cudaSuccess) return cuda_fail(e, "cluster cull launch");
-    c->launches++;
+    c->launches += 2;  // count, write
     return BLZ_OK;
 }
 

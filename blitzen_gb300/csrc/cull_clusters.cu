@@ -7,9 +7,11 @@
 // block takes a tile of objects, decides them and prefix-sums their cluster counts in shared
 // memory, then walks the tile's clusters in order (a binary search maps a cluster slot back to
 // its object), testing each one: sphere frustum, Hi-Z when a pyramid is bound, and the normal cone
-// in meshoptimizer's documented form (VendorCode/Meshoptimizer/meshoptimizer.h:561-569). A first
-// walk counts survivors for the decoupled look-back; a second walk recomputes the same tests and
-// writes records at their final slots, so nothing is materialised and the host never waits.
+// in meshoptimizer's documented form (VendorCode/Meshoptimizer/meshoptimizer.h:561-569).
+// Two launches, no block waiting on another: the count launch writes each tile's number of
+// surviving clusters; the write launch sums the counts of the tiles before its own (a strided
+// read), repeats the same tests and writes the records at their final slots. Nothing is
+// materialised and the host never waits.
 #include "blz_device.cuh"
 #include "kernels.h"
 
@@ -58,20 +60,16 @@ __device__ __forceinline__ bool cluster_visible(const ClusterParams& p, const Vi
     return vis;
 }
 
+template <bool WRITE>
 __global__ void __launch_bounds__(kClThreads) cull_clusters_kernel(const ClusterParams p, const BlzCameraViewData view) {
     __shared__ ClusterObj s_obj[kClObjects];
     __shared__ uint32_t s_start[kClObjects + 1];
     __shared__ uint32_t s_warp[kClWarps];
-    __shared__ uint32_t s_tile, s_epoch, s_base, s_total;
+    __shared__ uint32_t s_base;
     __shared__ unsigned int s_flags;
-    Scratch* scr = p.scratch;
-    if (threadIdx.x == 0) {
-        s_tile = atomicAdd(&scr->ticket, 1u);
-        s_epoch = *reinterpret_cast<volatile unsigned int*>(&scr->epoch);
-        s_flags = 0u;
-    }
+    if (threadIdx.x == 0) s_flags = 0u;
     __syncthreads();
-    const uint32_t tile = s_tile, epoch = s_epoch;
+    const uint32_t tile = blockIdx.x;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const ViewConsts v = load_view(view);
 
@@ -140,90 +138,93 @@ __global__ void __launch_bounds__(kClThreads) cull_clusters_kernel(const Cluster
     __syncthreads();
     const uint32_t T = s_start[kClObjects];
 
-    // walk 1: count survivors
-    uint32_t survivors = 0;
-    for (uint32_t slot = threadIdx.x; slot < T; slot += kClThreads) {
-        uint32_t lo = 0, hi = kClObjects;  // last object with start <= slot
-        while (hi - lo > 1u) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (s_start[mid] <= slot) lo = mid;
-            else hi = mid;
-        }
-        uint32_t ic, doff;
-        if (cluster_visible(p, v, s_obj[lo], s_obj[lo].clusterOffset + (slot - s_start[lo]), ic, doff)) ++survivors;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) survivors += __shfl_xor_sync(0xFFFFFFFFu, survivors, o);
-    if (lane == 0) s_warp[warp] = survivors;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t total = lane < kClWarps ? s_warp[lane] : 0u;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xFFFFFFFFu, total, o);
-        const uint32_t excl = lookback_warp(scr->state, tile, 0u, epoch, total, &scr->status);
-        if (lane == 0) {
-            s_base = excl;
-            s_total = total;
-        }
-    }
-    __syncthreads();
-
-    // walk 2: same tests, chunk by chunk in slot order, records at their final positions
-    uint32_t run = s_base;
-    const uint32_t lt = lanemask_lt();
-    for (uint32_t chunk = 0; chunk < T; chunk += kClThreads) {
-        const uint32_t slot = chunk + threadIdx.x;
-        bool vis = false;
-        uint32_t ic = 0, doff = 0, cid = 0, obj = 0;
-        if (slot < T) {
-            uint32_t lo = 0, hi = kClObjects;
+    if constexpr (!WRITE) {
+        // count the surviving clusters of the tile
+        uint32_t survivors = 0;
+        for (uint32_t slot = threadIdx.x; slot < T; slot += kClThreads) {
+            uint32_t lo = 0, hi = kClObjects;  // last object with start <= slot
             while (hi - lo > 1u) {
                 const uint32_t mid = (lo + hi) >> 1;
                 if (s_start[mid] <= slot) lo = mid;
                 else hi = mid;
             }
-            cid = s_obj[lo].clusterOffset + (slot - s_start[lo]);
-            obj = s_obj[lo].objectId;
-            vis = cluster_visible(p, v, s_obj[lo], cid, ic, doff);
+            uint32_t ic, doff;
+            if (cluster_visible(p, v, s_obj[lo], s_obj[lo].clusterOffset + (slot - s_start[lo]), ic, doff)) ++survivors;
         }
-        const unsigned b = __ballot_sync(0xFFFFFFFFu, vis);
-        __syncthreads();  // previous chunk's s_warp reads are done
-        if (lane == 0) s_warp[warp] = __popc(b);
-        __syncthreads();
-        uint32_t before = 0, chunkTotal = 0;
 #pragma unroll
-        for (int w = 0; w < kClWarps; ++w) {
-            const uint32_t c = s_warp[w];
-            if (w < static_cast<int>(warp)) before += c;
-            chunkTotal += c;
+        for (int o = 16; o > 0; o >>= 1) survivors += __shfl_xor_sync(0xFFFFFFFFu, survivors, o);
+        __syncthreads();  // every s_warp read of the scan above is done
+        if (lane == 0) s_warp[warp] = survivors;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t total = 0;
+            for (int w = 0; w < kClWarps; ++w) total += s_warp[w];
+            p.tileCount[tile] = total;
+            if (s_flags) atomicOr(&p.scratch->status, s_flags);
         }
-        if (vis) {
-            const uint32_t out = run + before + __popc(b & lt);
-            if (out < p.capacity) {
-                uint32_t* rec = reinterpret_cast<uint32_t*>(p.cmds + static_cast<size_t>(out) * p.stride);
-                rec[0] = obj;
-                rec[1] = ic;
-                rec[2] = 1u;
-                rec[3] = doff;
-                rec[4] = 0u;
-                rec[5] = 0u;
-                if (p.clusterIds) p.clusterIds[out] = cid;
+    } else {
+        // the records of the tiles before this one
+        uint32_t before = 0;
+        for (uint32_t t = threadIdx.x; t < tile; t += kClThreads) before += __ldcg(p.tileCount + t);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xFFFFFFFFu, before, o);
+        __syncthreads();  // every s_warp read of the scan above is done
+        if (lane == 0) s_warp[warp] = before;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t b = 0;
+            for (int w = 0; w < kClWarps; ++w) b += s_warp[w];
+            s_base = b;
+        }
+        __syncthreads();
+
+        // the tile's clusters in slot order, records at their final positions
+        uint32_t run = s_base;
+        const uint32_t lt = lanemask_lt();
+        for (uint32_t chunk = 0; chunk < T; chunk += kClThreads) {
+            const uint32_t slot = chunk + threadIdx.x;
+            bool vis = false;
+            uint32_t ic = 0, doff = 0, cid = 0, obj = 0;
+            if (slot < T) {
+                uint32_t lo = 0, hi = kClObjects;
+                while (hi - lo > 1u) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (s_start[mid] <= slot) lo = mid;
+                    else hi = mid;
+                }
+                cid = s_obj[lo].clusterOffset + (slot - s_start[lo]);
+                obj = s_obj[lo].objectId;
+                vis = cluster_visible(p, v, s_obj[lo], cid, ic, doff);
             }
+            const unsigned b = __ballot_sync(0xFFFFFFFFu, vis);
+            __syncthreads();  // the previous chunk's s_warp reads are done
+            if (lane == 0) s_warp[warp] = __popc(b);
+            __syncthreads();
+            uint32_t beforeW = 0, chunkTotal = 0;
+#pragma unroll
+            for (int w = 0; w < kClWarps; ++w) {
+                const uint32_t c = s_warp[w];
+                if (w < static_cast<int>(warp)) beforeW += c;
+                chunkTotal += c;
+            }
+            if (vis) {
+                const uint32_t out = run + beforeW + __popc(b & lt);
+                if (out < p.capacity) {
+                    uint32_t* rec = reinterpret_cast<uint32_t*>(p.cmds + static_cast<size_t>(out) * p.stride);
+                    rec[0] = obj;
+                    rec[1] = ic;
+                    rec[2] = 1u;
+                    rec[3] = doff;
+                    rec[4] = 0u;
+                    rec[5] = 0u;
+                    if (p.clusterIds) p.clusterIds[out] = cid;
+                }
+            }
+            run += chunkTotal;
         }
-        run += chunkTotal;
-    }
-    if (threadIdx.x == 0) {
-        unsigned int f = s_flags;
-        const uint32_t end = s_base + s_total;
-        if (end > p.capacity) f |= BLZ_FLAG_COMMAND_OVERFLOW;
-        if (f) atomicOr(&scr->status, f);
-        if (tile == gridDim.x - 1u) *p.drawCount = end;
-        __threadfence();
-        if (atomicAdd(&scr->doneBlocks, 1u) == gridDim.x - 1u) {
-            scr->ticket = 0u;
-            scr->doneBlocks = 0u;
-            __threadfence();
-            atomicExch(&scr->epoch, epoch + 1u);
+        if (threadIdx.x == 0 && tile == gridDim.x - 1u) {
+            *p.drawCount = run;
+            if (run > p.capacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
         }
     }
 }
@@ -233,7 +234,10 @@ uint32_t cluster_tile_objects() { return kClObjects; }
 cudaError_t launch_cluster_cull(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s) {
     uint32_t tiles = (p.count + kClObjects - 1) / kClObjects;
     if (tiles == 0) tiles = 1;
-    cull_clusters_kernel<<<tiles, kClThreads, 0, s>>>(p, view);
+    cull_clusters_kernel<false><<<tiles, kClThreads, 0, s>>>(p, view);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    cull_clusters_kernel<true><<<tiles, kClThreads, 0, s>>>(p, view);
     return cudaGetLastError();
 }
 

@@ -137,6 +137,7 @@ struct ClusterParams {
     uint32_t* clusterIds;
     uint32_t* drawCount;
     Scratch* scratch;
+    uint32_t* tileCount;  // scratch [tiles]: surviving clusters per tile
 };
 
 struct PyramidBuildParams {
