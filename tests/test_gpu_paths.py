@@ -60,6 +60,31 @@ def test_instanced_empty_view(stress_ctx):
     assert (dctr.cpu().numpy().view(np.uint32).reshape(-1, 2)[:, 1] == 0).all()
 
 
+@pytest.mark.parametrize("slots", [5_000, 7])
+def test_instanced_many_lods_matches_oracle(lib, slots):
+    """More LODs than the staged path keeps in shared memory (1,200): the single-kernel form runs."""
+    c = Culler(0)
+    try:
+        sc = S.frustum_lod_scene(60_000, seed=5, n_meshes=300, extent=800.0)
+        assert len(sc.lods) > 1024
+        c.setup_for_rendering(sc)
+        v = view_for(zfar=1e4)
+        ctr = O.new_counters(sc, slots)
+        cap = len(sc.lods) * slots
+        dctr = torch.from_numpy(ctr.view(np.int32).reshape(-1).copy()).cuda()
+        dinst = torch.full((cap,), -1, dtype=torch.int32, device="cuda")
+        t = Target.alloc(len(sc.lods), abi.STRIDE_D3D12)
+        c.draw_instance_cull_pass(v, dctr, dinst, slots, t)
+        flags = c.flags()
+        n, cmds, octr, oinst, oflags = O.cull_instanced(v, sc, ctr, cap, slots, stride=abi.STRIDE_D3D12)
+        assert flags == oflags
+        assert_records_equal(t.read(), (n, cmds), "instanced commands, 1,200 LODs")
+        assert np.array_equal(dctr.cpu().numpy().view(np.uint32), octr.view(np.uint32).reshape(-1))
+        assert np.array_equal(dinst.cpu().numpy().view(np.uint32), oinst)
+    finally:
+        c.close()
+
+
 # ----------------------------------------------------------------------------- raster + transforms
 
 def test_depth_raster_matches_oracle(stress_ctx):
@@ -165,6 +190,35 @@ def _batch(c, sc, n_views=12, seed=4, mode=abi.MODE_TEMPORAL):
         views[i].target = t.ctype()
         ref.append((v, objs, O.pyramid_build(depth), t))
     return views, keep, ref
+
+
+def test_batch_of_mixed_modes_matches_oracle(stress_ctx):
+    """One batch holding frustum, pass-1, pass-2 and temporal views (the mode is read per view)."""
+    c, sc = stress_ctx
+    views, keep, ref = _batch(c, sc, n_views=8, seed=13)
+    modes = [abi.MODE_FRUSTUM, abi.MODE_FIRST, abi.MODE_LATE, abi.MODE_TEMPORAL] * 2
+    vis_host = []
+    for i, m in enumerate(modes):
+        views[i].mode = m
+        if m in (abi.MODE_FIRST, abi.MODE_LATE):
+            vh = (np.random.default_rng(i).random(ref[i][1].shape[0]) < 0.5).astype(np.uint32)
+            vd = torch.from_numpy(vh.view(np.int32).copy()).cuda()
+            keep.append(vd)
+            views[i].visibility = vd.data_ptr()
+            vis_host.append((vh, vd))
+        else:
+            vis_host.append(None)
+    lib = abi.load()
+    abi.check(lib.blz_cull_batch(c.ctx, views, len(ref), None), "blz_cull_batch")
+    assert c.check() == 0
+    for i, (v, objs, opyr, t) in enumerate(ref):
+        m = modes[i]
+        ovis = vis_host[i][0].copy() if vis_host[i] is not None else None
+        n, recs, _ = O.cull(m, v, sc, objects=objs, vis=ovis,
+                            pyramid=opyr if m in (abi.MODE_LATE, abi.MODE_TEMPORAL) else None)
+        assert_records_equal(t.read(), (n, recs), f"view {i} mode {m}")
+        if m == abi.MODE_LATE:
+            assert np.array_equal(vis_host[i][1].cpu().numpy().view(np.uint32), ovis), f"view {i} visibility"
 
 
 @pytest.mark.parametrize("shape", [(256, 4, 0), (128, 1, 1), (512, 2, 0), (128, 8, 0), (256, 2, 2)])
