@@ -1,11 +1,11 @@
-// batch.cu — many views in one persistent launch, its per-view baseline, CUDA-graph replay and
-// the launch-shape autotuner.
+// batch.cu — many views in one launch, its per-view baseline, CUDA-graph replay, recorded frames
+// and the launch-shape autotuner.
 //
 // The reference culls one camera per pass with one dispatch each (src/Core/blitzenEngine.h:49,
-// src/Renderer/BlitzenVulkan/vulkanDraw.cpp:107-226). Here every (view, object tile) pair is an
-// item of one device work queue: persistent blocks take items from a ticket in view order and each
-// view keeps its own look-back chain, so views of 1k and 2M objects share the machine without a
-// launch or a tail per view.
+// src/Renderer/BlitzenVulkan/vulkanDraw.cpp:107-226). Here every (view, 512-object chunk) pair is
+// an item of one decide launch: warps start on the chunk of their index and take further chunks
+// from a work counter, and the scatter launch turns the per-chunk counts into per-view offsets and
+// draw counts, so views of 1k and 2M objects share the machine without a launch or a tail per view.
 #include <algorithm>
 #include <cstddef>
 #include <cstring>

@@ -309,80 +309,6 @@ __device__ __forceinline__ unsigned long long load_state(const unsigned long lon
     return v;
 }
 
-// Decoupled look-back by one warp: publishes this tile's aggregate, sums predecessors until an
-// inclusive prefix is found, publishes the inclusive prefix and returns the exclusive prefix.
-// Each round trip reads 128 predecessor states (four per lane, nearest first), so a chain of
-// hundreds of tiles that finished together resolves in a few L2 round trips.
-// Waits are bounded by kSpinLimit; on expiry the status word gets BLZ_FLAG_TIMEOUT and the partial
-// sum is used (the output is then flagged as invalid rather than the GPU waiting forever).
-// Tiles below firstTile belong to another chain (another view) and count as a zero prefix.
-// Publishes a tile's aggregate (or, for the first tile of a chain, its inclusive prefix).
-__device__ __forceinline__ void publish_aggregate(unsigned long long* states, uint32_t tile, uint32_t firstTile,
-                                                  uint32_t epoch, uint32_t aggregate) {
-    store_state(&states[tile], pack_state(epoch, tile == firstTile ? kStatePrefix : kStateAggregate, aggregate));
-}
-
-// The look-back half: sums the predecessors of a tile whose aggregate is already published, then
-// publishes its inclusive prefix. Called by one full warp; returns the exclusive prefix.
-__device__ __forceinline__ uint32_t resolve_prefix_warp(unsigned long long* states, uint32_t tile, uint32_t firstTile,
-                                                        uint32_t epoch, uint32_t aggregate, unsigned int* status) {
-    constexpr int kSub = 4;
-    const uint32_t lane = threadIdx.x & 31u;
-    if (tile == firstTile) return 0u;
-    uint32_t exclusive = 0;
-    int64_t window = static_cast<int64_t>(tile) - 1;  // sub-window j, lane l: tile window - 32 j - l
-    unsigned long long spins = 0;
-    while (true) {
-        uint32_t flag[kSub], value[kSub];
-#pragma unroll
-        for (int j = 0; j < kSub; ++j) {
-            const int64_t t = window - 32 * j - static_cast<int64_t>(lane);
-            flag[j] = kStatePrefix;  // tiles before firstTile act as a zero prefix
-            value[j] = 0u;
-            if (t >= static_cast<int64_t>(firstTile)) {
-                const unsigned long long s = load_state(&states[t]);
-                const uint32_t lo = static_cast<uint32_t>(s);
-                flag[j] = (static_cast<uint32_t>(s >> 32) == epoch) ? (lo >> 30) : 0u;
-                value[j] = lo & kValueMask;
-            }
-        }
-        int consumed = 0;
-        bool found = false;
-#pragma unroll
-        for (int j = 0; j < kSub; ++j) {
-            const unsigned notReady = __ballot_sync(0xFFFFFFFFu, flag[j] == 0u);
-            const unsigned prefixAt = __ballot_sync(0xFFFFFFFFu, flag[j] == kStatePrefix);
-            // lanes up to and including the nearest prefix (lowest lane with one) must be ready
-            const unsigned upto = prefixAt ? (prefixAt & (0u - prefixAt)) : 0u;
-            const unsigned need = prefixAt ? ((upto << 1) - 1u) : 0xFFFFFFFFu;
-            if (notReady & need) break;
-            uint32_t mine = ((need >> lane) & 1u) ? value[j] : 0u;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xFFFFFFFFu, mine, o);
-            exclusive += mine;
-            ++consumed;
-            if (prefixAt) {
-                found = true;
-                break;
-            }
-        }
-        if (found) break;
-        window -= 32 * consumed;
-        if (consumed < kSub && ++spins > kSpinLimit) {
-            if (lane == 0) atomicOr(status, BLZ_FLAG_TIMEOUT);
-            break;
-        }
-    }
-    if (lane == 0) store_state(&states[tile], pack_state(epoch, kStatePrefix, exclusive + aggregate));
-    return exclusive;
-}
-
-// Publish and resolve in one go (for kernels that have nothing to overlap with the wait).
-__device__ __forceinline__ uint32_t lookback_warp(unsigned long long* states, uint32_t tile, uint32_t firstTile,
-                                                  uint32_t epoch, uint32_t aggregate, unsigned int* status) {
-    if ((threadIdx.x & 31u) == 0) publish_aggregate(states, tile, firstTile, epoch, aggregate);
-    return resolve_prefix_warp(states, tile, firstTile, epoch, aggregate, status);
-}
 
 // One MeshTransform {pos.xyz, scale, quat.xyzw} in a single 256-bit read-only load (the table
 // is 32-byte aligned, checked on upload).
