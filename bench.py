@@ -65,6 +65,22 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(ms: float, world: int, device) -> float:
+    """The slowest rank's step time (each rank culls its own frame; the job takes the longest)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_throughput(objects_per_rank: int, world: int, ms: float) -> float:
+    """Objects per second of the whole job: every rank's objects over the slowest rank's time."""
+    return objects_per_rank * world / (ms * 1e-3)
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -298,13 +314,10 @@ def main():
     ms_first = [e[0].elapsed_time(e[1]) for e in evp]
     ms_pyr = [e[1].elapsed_time(e[2]) for e in evp]
     ms_late = [e[2].elapsed_time(e[3]) for e in evp]
-    t_step = sum(ms) / len(ms)
+    t_step = max_over_ranks(sum(ms) / len(ms), world, dev)
     if world > 1:
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
         dist.barrier()
-    value = N * world / (t_step * 1e-3)
+    value = job_throughput(N, world, t_step)
 
     # roofline of the dominant kernel (pass 2) and the others, algorithmic bytes
     stride = abi.STRIDE_VULKAN
@@ -359,20 +372,15 @@ def main():
             e1.synchronize()
             if k >= args.warmup:
                 out.append(e0.elapsed_time(e1))
-        t = sum(out) / len(out)
-        if world > 1:
-            tt = torch.tensor([t], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            t = float(tt.item())
-        return t
+        return max_over_ranks(sum(out) / len(out), world, dev)
 
     # the frame as a user replays it (the recorded frame through blz_graph_launch), and as direct calls
     t_e2e = e2e_run(frame.launch)
     t_e2e_direct = e2e_run(step_direct)
-    e2e = {"value": N * world / (t_e2e * 1e-3), "unit": "objects/s", "ms_per_step": t_e2e,
+    e2e = {"value": job_throughput(N, world, t_e2e), "unit": "objects/s", "ms_per_step": t_e2e,
            "h2d_bytes_per_step": W * H * 4 + DYNAMIC * (32 + 4), "d2h_bytes_per_step": 8,
            "path": "blz_transforms_update + depth H2D + blz_graph_launch(recorded frame) + count D2H",
-           "direct_calls": {"value": N * world / (t_e2e_direct * 1e-3), "ms_per_step": t_e2e_direct,
+           "direct_calls": {"value": job_throughput(N, world, t_e2e_direct), "ms_per_step": t_e2e_direct,
                             "path": "same, with blz_cull_first / blz_pyramid_build / blz_cull_late called directly"}}
 
     extras = {}
