@@ -2,10 +2,12 @@
 //
 // The reference builds the pyramid with one dispatch per mip and a barrier between them
 // (src/Renderer/BlitzenDX12/dx12Draw.cpp:248-277, src/Renderer/BlitzenVulkan/vulkanDraw.cpp:579-614).
-// Here one launch builds every mip: each block owns a 32x32 tile of mip 0 (every load of the tile
-// issued before any is used), writes it, and reduces it through mips 1..5 in shared memory (a
-// 32-texel tile reaches 1 texel at mip 5); the last block to finish (device counter) reads mip 5
-// into shared memory when it fits and builds the few remaining small mips there.
+// Here two launches build every mip: in the first, each block owns a 32x32 tile of mip 0 (every load
+// of the tile issued before any is used), writes it, and reduces it through mips 1..5 in shared
+// memory (a 32-texel tile reaches 1 texel at mip 5); the second, one block, reads mip 5 into
+// shared memory when it fits and builds the few remaining small mips there. (A last-block-finishes
+// form in one launch measured slower: every block fenced its writes and 510 blocks queued on one
+// counter.)
 //
 // Texel rules:
 //   D3D12   depthPyramid.cs.hlsl:16-26 — min(r, min(g, min(b, a))) of the 2x2 Loads at
@@ -21,6 +23,7 @@
 namespace blz {
 
 constexpr int kPyrThreads = 256;
+constexpr int kPyrTopThreads = 1024;
 constexpr uint32_t kPyrTile = 32;
 constexpr uint32_t kPyrInTileLevels = 5;
 constexpr uint32_t kPyrPerThread = kPyrTile * kPyrTile / kPyrThreads;  // mip-0 texels per thread
@@ -74,8 +77,6 @@ template <uint32_t MODE>
 __global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuildParams p) {
     __shared__ float sA[kPyrTile * kPyrTile];
     __shared__ float sB[(kPyrTile / 2) * (kPyrTile / 2)];
-    __shared__ float sTop[2][kPyrTopTexels];
-    __shared__ int s_last;
     const uint32_t X0 = blockIdx.x * kPyrTile, Y0 = blockIdx.y * kPyrTile;
     const uint32_t W0 = p.width, H0 = p.height;
 
@@ -166,22 +167,20 @@ __global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuild
         S = Sk;
     }
 
-    if (p.mipCount <= kPyrInTileLevels + 1) return;
+}
 
-    // the last block to finish builds the small mips that span several tiles
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = (atomicAdd(p.counter, 1u) == gridDim.x * gridDim.y - 1u) ? 1 : 0;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
+// The mips above level 5, which span several tiles, by one block.
+template <uint32_t MODE>
+__global__ void __launch_bounds__(kPyrTopThreads) pyramid_top_kernel(const PyramidBuildParams p) {
+    __shared__ float sTop[2][kPyrTopTexels];
+    const uint32_t W0 = p.width, H0 = p.height;
     uint32_t k = kPyrInTileLevels + 1;
     {
         // the level every tile finished, then the rest in shared memory while they fit
         const uint32_t Wt = mip_dim(W0, kPyrInTileLevels), Ht = mip_dim(H0, kPyrInTileLevels);
         if (Wt * Ht <= kPyrTopTexels) {
             const float* top = p.data + p.mipOffset[kPyrInTileLevels];
-            for (uint32_t i = threadIdx.x; i < Wt * Ht; i += kPyrThreads) sTop[0][i] = __ldcg(top + i);
+            for (uint32_t i = threadIdx.x; i < Wt * Ht; i += kPyrTopThreads) sTop[0][i] = __ldcg(top + i);
             __syncthreads();
             int cur = 0;
             for (; k < p.mipCount; ++k) {
@@ -190,7 +189,7 @@ __global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuild
                 const float* prev = sTop[cur];
                 float* next = sTop[cur ^ 1];
                 float* out = p.data + p.mipOffset[k];
-                for (uint32_t idx = threadIdx.x; idx < Wk * Hk; idx += kPyrThreads) {
+                for (uint32_t idx = threadIdx.x; idx < Wk * Hk; idx += kPyrTopThreads) {
                     const uint32_t gx = idx % Wk, gy = idx / Wk;
                     float t;
                     if (MODE == BLZ_HIZ_D3D12) {
@@ -219,26 +218,31 @@ __global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuild
             }
         }
     }
-    for (; k < p.mipCount; ++k) {
+    for (; k < p.mipCount; ++k) {  // levels too large for shared memory, through global memory
         const uint32_t Wp = mip_dim(W0, k - 1), Hp = mip_dim(H0, k - 1);
         const uint32_t Wk = mip_dim(W0, k), Hk = mip_dim(H0, k);
         const float* prev = p.data + p.mipOffset[k - 1];
         float* out = p.data + p.mipOffset[k];
-        for (uint32_t idx = threadIdx.x; idx < Wk * Hk; idx += kPyrThreads) {
+        for (uint32_t idx = threadIdx.x; idx < Wk * Hk; idx += kPyrTopThreads) {
             const uint32_t gx = idx % Wk, gy = idx / Wk;
             out[idx] = level_texel_global<MODE>(prev, Wp, Hp, gx, gy, Wk, Hk);
         }
         __threadfence_block();
         __syncthreads();
     }
-    if (threadIdx.x == 0) *p.counter = 0u;
 }
 
 cudaError_t launch_pyramid_build(const PyramidBuildParams& p, cudaStream_t s, uint32_t* launches) {
     dim3 grid((p.width + kPyrTile - 1) / kPyrTile, (p.height + kPyrTile - 1) / kPyrTile);
-    if (p.mode == BLZ_HIZ_VULKAN) pyramid_kernel<BLZ_HIZ_VULKAN><<<grid, kPyrThreads, 0, s>>>(p);
-    else pyramid_kernel<BLZ_HIZ_D3D12><<<grid, kPyrThreads, 0, s>>>(p);
-    if (launches) *launches += 1;
+    const bool top = p.mipCount > kPyrInTileLevels + 1;
+    if (p.mode == BLZ_HIZ_VULKAN) {
+        pyramid_kernel<BLZ_HIZ_VULKAN><<<grid, kPyrThreads, 0, s>>>(p);
+        if (top) pyramid_top_kernel<BLZ_HIZ_VULKAN><<<1, kPyrTopThreads, 0, s>>>(p);
+    } else {
+        pyramid_kernel<BLZ_HIZ_D3D12><<<grid, kPyrThreads, 0, s>>>(p);
+        if (top) pyramid_top_kernel<BLZ_HIZ_D3D12><<<1, kPyrTopThreads, 0, s>>>(p);
+    }
+    if (launches) *launches += top ? 2u : 1u;
     return cudaGetLastError();
 }
 
