@@ -371,6 +371,22 @@ __global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const 
     if (c0 >= p.totalTiles) return;
     const uint32_t vi0 = SINGLE ? 0u : find_view(p.tileStart, p.viewCount, c0);
     const uint32_t viewStart0 = SINGLE ? 0u : __ldg(p.tileStart + vi0);
+    // 0. each warp fetches its chunk's first 2 * 32 staged records and their LODs now, so those
+    //    loads overlap the offset computation below
+    const uint32_t myChunk = c0 + warp;
+    const uint32_t myN = myChunk < p.totalTiles ? __ldcg(p.chunkCount + myChunk) : 0u;
+    const uint2* myStage = p.staged + static_cast<size_t>(myChunk) * chunkSize;
+    uint2 pre[2], preLod[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const uint32_t i = lane + 32u * u;
+        pre[u] = i < myN ? __ldcg(myStage + i) : make_uint2(0u, 0u);
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const uint32_t i = lane + 32u * u;
+        preLod[u] = i < myN ? __ldg(reinterpret_cast<const uint2*>(p.sc.lods + pre[u].y)) : make_uint2(0u, 0u);
+    }
     // 1. records of the first chunk's view before c0
     uint32_t part = 0;
     for (uint32_t c = viewStart0 + threadIdx.x; c < c0; c += kScatterWarps * 32) part += __ldcg(p.chunkCount + c);
@@ -421,20 +437,22 @@ __global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const 
         }
     }
     __syncthreads();
-    // 3. scatter, one chunk per warp at a time
-    for (uint32_t j = warp; j < kScatterChunks; j += kScatterWarps) {
-        const uint32_t chunk = c0 + j;
-        if (chunk >= p.totalTiles) break;
-        const uint32_t n = s_n[j], base = s_base[j];
-        const BatchViewDev& bv = view_of<SINGLE>(p, s_vi[j]);
-        const uint2* stage = p.staged + static_cast<size_t>(chunk) * chunkSize;
-        for (uint32_t i = lane; i < n; i += 32) {
-            const uint32_t slot = base + i;
-            if (slot >= bv.capacity) break;
-            const uint2 rec = __ldcg(stage + i);
-            const uint2 lod = __ldg(reinterpret_cast<const uint2*>(p.sc.lods + rec.y));  // indexCount, firstIndex
-            put_record(bv.cmds, bv.stride, slot, rec.x, lod.x, lod.y);
-        }
+    // 3. scatter: each warp its own chunk (kScatterWarps == kScatterChunks)
+    static_assert(kScatterWarps == static_cast<int>(kScatterChunks), "one warp per chunk");
+    if (myChunk >= p.totalTiles) return;
+    const uint32_t base = s_base[warp];
+    const BatchViewDev& bv = view_of<SINGLE>(p, s_vi[warp]);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const uint32_t i = lane + 32u * u;
+        if (i < myN && base + i < bv.capacity) put_record(bv.cmds, bv.stride, base + i, pre[u].x, preLod[u].x, preLod[u].y);
+    }
+    for (uint32_t i = lane + 64u; i < myN; i += 32) {
+        const uint32_t slot = base + i;
+        if (slot >= bv.capacity) break;
+        const uint2 rec = __ldcg(myStage + i);
+        const uint2 lod = __ldg(reinterpret_cast<const uint2*>(p.sc.lods + rec.y));  // indexCount, firstIndex
+        put_record(bv.cmds, bv.stride, slot, rec.x, lod.x, lod.y);
     }
 }
 
