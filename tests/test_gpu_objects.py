@@ -200,3 +200,54 @@ def test_deterministic_rerun(sculler, stress):
 
 
 O_FIRST, O_LATE, O_TEMPORAL = 1, 2, 3
+
+
+def test_recorded_frame_replays_match_direct_calls(culler, c1):
+    """A frame recorded with blz_capture_begin/end and replayed with blz_graph_launch gives the
+    same records and visibility as the direct calls, replay after replay."""
+    v = view_for(zfar=3000.0, yaw=0.4)
+    depth = torch.from_numpy(O.depth_raster(v, S.make_occluders(np.random.default_rng(3), 300), W, H)).cuda()
+    vis0 = (np.random.default_rng(4).random(c1.count) < 0.5).astype(np.uint32)
+    vis = torch.from_numpy(vis0.view(np.int32).copy()).cuda()
+    t1, t2 = Target.alloc(c1.count), Target.alloc(c1.count)
+    pyr = DevicePyramid(W, H)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        culler.draw_cull_first_pass(v, vis, t1)
+        culler.generate_depth_pyramid(pyr, depth)
+        culler.draw_cull_occlusion_pass(v, vis, pyr, t2)
+        side.synchronize()
+        want = (t1.read(), t2.read(), vis.cpu().numpy().copy())
+        culler.capture_begin()
+        culler.draw_cull_first_pass(v, vis, t1)
+        culler.generate_depth_pyramid(pyr, depth)
+        culler.draw_cull_occlusion_pass(v, vis, pyr, t2)
+        g = culler.capture_end()
+        try:
+            assert g.kernels >= 5
+            for rep in range(3):
+                vis.copy_(torch.from_numpy(vis0.view(np.int32).copy()).cuda())
+                t1.count.fill_(0)
+                t2.count.fill_(0)
+                g.launch()
+                side.synchronize()
+                assert_records_equal(t1.read(), want[0], f"replay {rep} pass 1")
+                assert_records_equal(t2.read(), want[1], f"replay {rep} pass 2")
+                assert np.array_equal(vis.cpu().numpy(), want[2])
+        finally:
+            g.close()
+    assert culler.check(side) == 0
+
+
+def test_capture_refuses_to_grow_scratch(culler, c1):
+    """Scratch cannot be allocated inside a capture: a list longer than any run before is refused."""
+    big = to_device(np.tile(c1.objects, 40), "cuda")  # more chunks than the context has seen
+    t = Target.alloc(16)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        culler.capture_begin()
+        with pytest.raises(abi.BlzError) as ei:
+            culler.draw_cull(view_for(), t, objects=big, count=c1.count * 40)
+        g = culler.capture_end()
+        g.close()
+    assert ei.value.code == 2  # BLZ_ERR_CAPACITY
