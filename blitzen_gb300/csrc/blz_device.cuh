@@ -319,6 +319,14 @@ __device__ __forceinline__ void ldg_transform(const BlzMeshTransform* t, float4&
         : "l"(t));
 }
 
+// Programmatic dependent launch. A kernel launched with programmatic stream serialization may be
+// scheduled while the kernel before it on the stream is still finishing; pdl_wait() holds it,
+// before it touches any memory, until that kernel has completed and its writes are visible (a
+// kernel launched without the attribute passes straight through). pdl_launch_next() lets the
+// next kernel on the stream be scheduled now, to wait in its own pdl_wait().
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_next() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

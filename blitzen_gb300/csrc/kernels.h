@@ -149,6 +149,24 @@ struct PyramidBuildParams {
     unsigned int* counter;   // scratch: blocks finished
 };
 
+// Launches a kernel with programmatic stream serialization: it may be scheduled while the kernel
+// before it on the stream finishes, and waits in pdl_wait() before touching memory.
+template <typename... Params, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Params>(args)...);
+}
+
 uint32_t object_tile_size();
 // Chunk size of a single-view launch of `count` objects: one chunk per warp the launch holds
 // resident, so every warp streams one contiguous run of objects and none waits for a second round.

@@ -77,6 +77,8 @@ template <uint32_t MODE>
 __global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuildParams p) {
     __shared__ float sA[kPyrTile * kPyrTile];
     __shared__ float sB[(kPyrTile / 2) * (kPyrTile / 2)];
+    pdl_wait();
+    pdl_launch_next();
     const uint32_t X0 = blockIdx.x * kPyrTile, Y0 = blockIdx.y * kPyrTile;
     const uint32_t W0 = p.width, H0 = p.height;
 
@@ -173,6 +175,8 @@ __global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuild
 template <uint32_t MODE>
 __global__ void __launch_bounds__(kPyrTopThreads) pyramid_top_kernel(const PyramidBuildParams p) {
     __shared__ float sTop[2][kPyrTopTexels];
+    pdl_wait();
+    pdl_launch_next();
     const uint32_t W0 = p.width, H0 = p.height;
     uint32_t k = kPyrInTileLevels + 1;
     {
@@ -235,15 +239,16 @@ __global__ void __launch_bounds__(kPyrTopThreads) pyramid_top_kernel(const Pyram
 cudaError_t launch_pyramid_build(const PyramidBuildParams& p, cudaStream_t s, uint32_t* launches) {
     dim3 grid((p.width + kPyrTile - 1) / kPyrTile, (p.height + kPyrTile - 1) / kPyrTile);
     const bool top = p.mipCount > kPyrInTileLevels + 1;
+    cudaError_t e;
     if (p.mode == BLZ_HIZ_VULKAN) {
-        pyramid_kernel<BLZ_HIZ_VULKAN><<<grid, kPyrThreads, 0, s>>>(p);
-        if (top) pyramid_top_kernel<BLZ_HIZ_VULKAN><<<1, kPyrTopThreads, 0, s>>>(p);
+        e = launch_pdl(pyramid_kernel<BLZ_HIZ_VULKAN>, grid, dim3(kPyrThreads), 0, s, p);
+        if (e == cudaSuccess && top) e = launch_pdl(pyramid_top_kernel<BLZ_HIZ_VULKAN>, dim3(1), dim3(kPyrTopThreads), 0, s, p);
     } else {
-        pyramid_kernel<BLZ_HIZ_D3D12><<<grid, kPyrThreads, 0, s>>>(p);
-        if (top) pyramid_top_kernel<BLZ_HIZ_D3D12><<<1, kPyrTopThreads, 0, s>>>(p);
+        e = launch_pdl(pyramid_kernel<BLZ_HIZ_D3D12>, grid, dim3(kPyrThreads), 0, s, p);
+        if (e == cudaSuccess && top) e = launch_pdl(pyramid_top_kernel<BLZ_HIZ_D3D12>, dim3(1), dim3(kPyrTopThreads), 0, s, p);
     }
     if (launches) *launches += top ? 2u : 1u;
-    return cudaGetLastError();
+    return e;
 }
 
 }  // namespace blz
