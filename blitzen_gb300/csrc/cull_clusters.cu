@@ -19,7 +19,7 @@ namespace blz {
 
 constexpr int kClThreads = 256;
 constexpr int kClWarps = kClThreads / 32;
-constexpr uint32_t kClObjects = 64;  // objects per tile
+constexpr uint32_t kClObjects = 32;  // objects per tile
 
 struct ClusterObj {
     float4 posScale;
@@ -28,9 +28,11 @@ struct ClusterObj {
     uint32_t clusterOffset;
 };
 
-// Sphere, Hi-Z and cone tests of one cluster of an object.
+// Sphere, Hi-Z and cone tests of one cluster of an object. snorm[i] holds (float)(i - 128) / 127,
+// divided once per block: the int8 cone axis and cutoff take only those 256 values.
 __device__ __forceinline__ bool cluster_visible(const ClusterParams& p, const ViewConsts& v, const ClusterObj& o,
-                                                uint32_t cid, uint32_t& indexCount, uint32_t& dataOffset) {
+                                                uint32_t cid, const float* snorm, uint32_t& indexCount,
+                                                uint32_t& dataOffset) {
     const float4* cp = reinterpret_cast<const float4*>(p.sc.clusters + cid);
     const float4 sph = __ldg(cp);
     const uint4 meta = __ldg(reinterpret_cast<const uint4*>(cp + 1));  // cone s8x4, dataOffset, counts, pad
@@ -45,9 +47,8 @@ __device__ __forceinline__ bool cluster_visible(const ClusterParams& p, const Vi
     if (vis) {
         const int ax = static_cast<int8_t>(meta.x & 0xFFu), ay = static_cast<int8_t>((meta.x >> 8) & 0xFFu);
         const int az = static_cast<int8_t>((meta.x >> 16) & 0xFFu), ac = static_cast<int8_t>(meta.x >> 24);
-        const Vec3 axm{BLZ_FD(static_cast<float>(ax), 127.0f), BLZ_FD(static_cast<float>(ay), 127.0f),
-                       BLZ_FD(static_cast<float>(az), 127.0f)};
-        const float cutoff = BLZ_FD(static_cast<float>(ac), 127.0f);
+        const Vec3 axm{snorm[ax + 128], snorm[ay + 128], snorm[az + 128]};
+        const float cutoff = snorm[ac + 128];
         const Vec3 axis = rotate_quat(axm, o.quat);
         const float dx = BLZ_FS(w.x, v.camX), dy = BLZ_FS(w.y, v.camY), dz = BLZ_FS(w.z, v.camZ);
         const float len = __fsqrt_rn(BLZ_FA(BLZ_FA(BLZ_FM(dx, dx), BLZ_FM(dy, dy)), BLZ_FM(dz, dz)));
@@ -67,7 +68,10 @@ __global__ void __launch_bounds__(kClThreads) cull_clusters_kernel(const Cluster
     __shared__ uint32_t s_warp[kClWarps];
     __shared__ uint32_t s_base;
     __shared__ unsigned int s_flags;
+    __shared__ float s_snorm[256];
     if (threadIdx.x == 0) s_flags = 0u;
+    for (uint32_t i = threadIdx.x; i < 256u; i += kClThreads)
+        s_snorm[i] = BLZ_FD(static_cast<float>(static_cast<int>(i) - 128), 127.0f);
     __syncthreads();
     const uint32_t tile = blockIdx.x;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -121,8 +125,10 @@ __global__ void __launch_bounds__(kClThreads) cull_clusters_kernel(const Cluster
         s_obj[threadIdx.x] = o;
     }
     if (flags) atomicOr(&s_flags, flags);
-    // exclusive scan of the per-object cluster counts (warps 0 and 1 hold the 64 objects)
-    if (warp < 2) {
+    // exclusive scan of the per-object cluster counts (the first kClObjects / 32 warps hold them)
+    constexpr uint32_t kObjWarps = kClObjects / 32;
+    static_assert(kClObjects % 32 == 0 && kObjWarps >= 1 && kObjWarps <= 2, "one or two warps of objects");
+    if (warp < kObjWarps) {
         uint32_t incl = count;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -134,7 +140,7 @@ __global__ void __launch_bounds__(kClThreads) cull_clusters_kernel(const Cluster
     }
     __syncthreads();
     if (threadIdx.x >= 32 && threadIdx.x < kClObjects) s_start[threadIdx.x] += s_warp[0];
-    if (threadIdx.x == 0) s_start[kClObjects] = s_warp[0] + s_warp[1];
+    if (threadIdx.x == 0) s_start[kClObjects] = kObjWarps == 2 ? s_warp[0] + s_warp[1] : s_warp[0];
     __syncthreads();
     const uint32_t T = s_start[kClObjects];
 
@@ -149,7 +155,7 @@ __global__ void __launch_bounds__(kClThreads) cull_clusters_kernel(const Cluster
                 else hi = mid;
             }
             uint32_t ic, doff;
-            if (cluster_visible(p, v, s_obj[lo], s_obj[lo].clusterOffset + (slot - s_start[lo]), ic, doff)) ++survivors;
+            if (cluster_visible(p, v, s_obj[lo], s_obj[lo].clusterOffset + (slot - s_start[lo]), s_snorm, ic, doff)) ++survivors;
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) survivors += __shfl_xor_sync(0xFFFFFFFFu, survivors, o);
@@ -194,7 +200,7 @@ __global__ void __launch_bounds__(kClThreads) cull_clusters_kernel(const Cluster
                 }
                 cid = s_obj[lo].clusterOffset + (slot - s_start[lo]);
                 obj = s_obj[lo].objectId;
-                vis = cluster_visible(p, v, s_obj[lo], cid, ic, doff);
+                vis = cluster_visible(p, v, s_obj[lo], cid, s_snorm, ic, doff);
             }
             const unsigned b = __ballot_sync(0xFFFFFFFFu, vis);
             __syncthreads();  // the previous chunk's s_warp reads are done
