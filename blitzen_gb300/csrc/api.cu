@@ -174,7 +174,6 @@ int blz_ctx_destroy(blz_ctx* c) {
     if (c->pinned) cudaFreeHost(c->pinned);
     if (c->pinnedDone) cudaEventDestroy(c->pinnedDone);
     if (c->batchDev) cudaFree(c->batchDev);
-    if (c->stagingDev) cudaFree(c->stagingDev);
     if (c->chunkMem) cudaFree(c->chunkMem);
     if (c->instScratch) cudaFree(c->instScratch);
     delete c;
@@ -302,18 +301,19 @@ int blz_transforms_update(blz_ctx* c, const uint32_t* ids, const BlzMeshTransfor
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const size_t need = (size_t)n * (sizeof(uint32_t) + sizeof(BlzMeshTransform)) + 64;
     if (need > kPinnedBytes) return fail(BLZ_ERR_CAPACITY, "%u transforms exceed the staging buffer", n);
-    int rc = ensure_staging(c, need);
-    if (rc != BLZ_OK) return rc;
-    cudaEventSynchronize(c->pinnedDone);  // the previous staged copy has left the pinned buffer
+    cudaEventSynchronize(c->pinnedDone);  // the previous update's kernel has read the pinned buffer
     char* h = static_cast<char*>(c->pinned);
     const size_t tOff = 0, iOff = ((size_t)n * sizeof(BlzMeshTransform) + 63) & ~size_t(63);
     memcpy(h + tOff, in, (size_t)n * sizeof(BlzMeshTransform));
     memcpy(h + iOff, ids, (size_t)n * sizeof(uint32_t));
-    char* d = static_cast<char*>(c->stagingDev);
-    cudaError_t e = cudaMemcpyAsync(d, h, iOff + (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaEventRecord(c->pinnedDone, st);
-    if (e != cudaSuccess) return cuda_fail(e, "transform staging copy");
-    return blz_transforms_update_device(c, reinterpret_cast<const uint32_t*>(d + iOff), reinterpret_cast<const BlzMeshTransform*>(d + tOff), n, stream);
+    // the scatter kernel reads the rows straight from pinned host memory (no staging copy): over
+    // the coherent CPU-GPU link of a Grace-Blackwell node that is one transfer instead of two
+    int rc = blz_transforms_update_device(c, reinterpret_cast<const uint32_t*>(h + iOff),
+                                          reinterpret_cast<const BlzMeshTransform*>(h + tOff), n, stream);
+    if (rc != BLZ_OK) return rc;
+    cudaError_t e = cudaEventRecord(c->pinnedDone, st);
+    if (e != cudaSuccess) return cuda_fail(e, "transform update event");
+    return BLZ_OK;
 }
 
 int blz_transforms_rotate(blz_ctx* c, const uint32_t* ids, const float* axes, float angle, uint32_t n, BlzMeshTransform* dst,

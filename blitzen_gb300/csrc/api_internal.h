@@ -13,7 +13,7 @@
 namespace blz {
 
 constexpr size_t kDefaultStateCapacity = size_t(1) << 22;  // 4M tile states (32 MiB)
-constexpr size_t kPinnedBytes = size_t(8) << 20;            // transform / batch staging
+constexpr size_t kPinnedBytes = size_t(8) << 20;            // pinned host staging: transform rows, batch views
 constexpr uint32_t kMaxInstancedLods = 4096;                // shared-memory bucket histograms
 
 }  // namespace blz
@@ -27,8 +27,6 @@ struct blz_ctx {
     unsigned int* pyrCounter = nullptr;
     void* pinned = nullptr;            // pinned host staging
     cudaEvent_t pinnedDone = nullptr;  // last copy out of `pinned` has completed
-    void* stagingDev = nullptr;        // device side of the staging
-    size_t stagingBytes = 0;
     void* batchDev = nullptr;          // device BatchViewDev[] + tileStart[]
     size_t batchBytes = 0;
     void* chunkMem = nullptr;          // object-cull staging: records, chunk counts
@@ -62,21 +60,5 @@ int ensure_states(blz_ctx* c, size_t states);
 // grows it synchronises the device first).
 int ensure_chunk_scratch(blz_ctx* c, size_t chunks, size_t chunkSize);
 void bind_chunk_scratch(blz_ctx* c, PipeParams& p);
-
-inline int ensure_staging(blz_ctx* c, size_t bytes) {
-    if (bytes <= c->stagingBytes) return 0;
-    if (c->stagingDev) {
-        cudaStreamSynchronize(nullptr);
-        cudaDeviceSynchronize();
-        cudaFree(c->stagingDev);
-        c->stagingDev = nullptr;
-        c->stagingBytes = 0;
-    }
-    size_t want = bytes < kPinnedBytes ? kPinnedBytes : bytes;
-    cudaError_t e = cudaMalloc(&c->stagingDev, want);
-    if (e != cudaSuccess) return fail(BLZ_ERR_OUT_OF_MEMORY, "staging allocation of %zu bytes failed", want);
-    c->stagingBytes = want;
-    return 0;
-}
 
 }  // namespace blz

@@ -158,6 +158,12 @@ class Culler:
         check(self.lib.blz_transforms_update(self.ctx, ids.ctypes.data, tr.ctypes.data, len(ids), _stream_ptr(stream)),
               "blz_transforms_update")
 
+    def update_object_transform_device(self, ids: torch.Tensor, transforms: torch.Tensor, stream=None) -> None:
+        """UpdateObjectTransform from device-accessible buffers (device memory, or pinned host memory
+        the kernel reads directly); recordable in a graph."""
+        check(self.lib.blz_transforms_update_device(self.ctx, ids.data_ptr(), transforms.data_ptr(),
+                                                    ids.numel(), _stream_ptr(stream)), "blz_transforms_update_device")
+
     def rotate_transforms(self, ids: torch.Tensor, axes: torch.Tensor, angle: float, dst: torch.Tensor, stream=None):
         check(self.lib.blz_transforms_rotate(self.ctx, ids.data_ptr(), axes.data_ptr(), angle, ids.numel(),
                                              dst.data_ptr(), _stream_ptr(stream)), "blz_transforms_rotate")

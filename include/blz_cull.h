@@ -161,10 +161,12 @@ typedef struct BlzPyramid {
  * (src/BlitzenMathLibrary/blitML.h:95-107). */
 uint64_t blz_pyramid_layout(uint32_t depthWidth, uint32_t depthHeight, uint32_t mode, BlzPyramid* out);
 
-/* Builds every mip from a device fp32 reverse-Z depth buffer (row-major, depthWidth floats per
- * row) in one single-pass launch. Replaces GenerateDepthPyramid
+/* Builds every mip from an fp32 reverse-Z depth buffer (row-major, depthWidth floats per row):
+ * one launch for the 32x32 tiles and one for the top mips. Replaces GenerateDepthPyramid
  * (src/Renderer/BlitzenDX12/dx12Draw.cpp:224-288, src/Renderer/BlitzenVulkan/vulkanDraw.cpp:554-622)
- * and its per-mip dispatches of depthPyramid.cs.hlsl / DepthPyramidGeneration.comp.glsl. */
+ * and its per-mip dispatches of depthPyramid.cs.hlsl / DepthPyramidGeneration.comp.glsl.
+ * dDepth is any device-accessible pointer: device memory, or pinned host memory that the kernel
+ * then reads once over the CPU-GPU link (no separate upload). */
 int blz_pyramid_build(blz_ctx* ctx, const BlzPyramid* pyramid, const float* dDepth, blz_stream_t stream);
 
 /* Rasterises axis-aligned occluder boxes (world space, 6 floats each: min xyz, max xyz) into a
@@ -185,7 +187,8 @@ typedef struct BlzCullTarget {
     void* commands;          /* device: records of `stride` bytes */
     uint32_t stride;         /* BLZ_STRIDE_VULKAN or BLZ_STRIDE_D3D12 */
     uint32_t capacity;       /* records the buffer can hold */
-    uint32_t* drawCount;     /* device: set to the number of visible records (not accumulated) */
+    uint32_t* drawCount;     /* device-accessible (device or pinned host memory): set to the number
+                              * of visible records (not accumulated) */
 } BlzCullTarget;
 
 /* Frustum + LOD cull of every object, no occlusion, no visibility state.
