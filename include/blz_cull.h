@@ -123,12 +123,13 @@ int blz_scene_upload(blz_ctx* ctx, const BlzSceneDesc* scene, uint32_t flags, bl
 int blz_scene_device_tables(const blz_ctx* ctx, BlzSceneDesc* out);
 
 /* Overwrites transforms[ids[i]] = transforms_in[i] for i < n. ids and transforms_in are host
- * arrays (staged through pinned memory). Replaces UpdateObjectTransform + UpdateBuffers
- * (src/Renderer/BlitzenVulkan/vulkanDraw.cpp:46-60,816-820). */
+ * arrays, copied into the context's pinned buffer, which the update kernel reads directly.
+ * Replaces UpdateObjectTransform + UpdateBuffers (src/Renderer/BlitzenVulkan/vulkanDraw.cpp:46-60,816-820). */
 int blz_transforms_update(blz_ctx* ctx, const uint32_t* ids, const BlzMeshTransform* transformsIn,
                           uint32_t n, blz_stream_t stream);
 
-/* Same, with ids and transforms already in device memory. */
+/* Same, with ids and transforms in device-accessible memory (device memory, or pinned host memory
+ * the kernel reads directly); recordable in a captured frame. */
 int blz_transforms_update_device(blz_ctx* ctx, const uint32_t* dIds, const BlzMeshTransform* dTransforms,
                                  uint32_t n, blz_stream_t stream);
 
