@@ -419,7 +419,11 @@ def main():
         counts = hcounts0.numpy().copy()  # the step's result, already in host memory
         if k >= args.warmup:
             zc_ms.append(e0.elapsed_time(e1))
-    assert int(counts[0]) == V1 and int(counts[1]) == V2, (counts, V1, V2)
+    # the recorded step's counts (written to host memory) equal a direct run on the same state
+    vis.copy_(vis0)
+    step_direct()
+    torch.cuda.synchronize()
+    assert (int(counts[0]), int(counts[1])) == (t1.read()[0], t2.read()[0]), counts
     t_e2e = max_over_ranks(sum(zc_ms) / len(zc_ms), world, dev)
     frame_zc.close()
     e2e = {"value": job_throughput(N, world, t_e2e), "unit": "objects/s", "ms_per_step": t_e2e,

@@ -74,7 +74,7 @@ __device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchVi
         a = e[0];
         b = e[1];
     }
-    const uint32_t obj = a.x & 0x7FFFFFFFu;
+    const uint32_t obj = a.x & 0x3FFFFFFFu;  // LATE: bit 31 previous visibility != 0, bit 30 == 1
     const Vec3 c{__uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(a.w)};
     const float r = __uint_as_float(b.x), scale = __uint_as_float(b.y);
     bool visible = mine;
@@ -83,7 +83,11 @@ __device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchVi
             float4 aabb;
             if (project_sphere(c, r, v.zNear, v.proj0, v.proj5, aabb)) visible = occlusion(aabb, bv.pyr, v, c, r);
         }
-        if (MODE == BLZ_MODE_LATE) bv.vis[obj] = visible ? 1u : 0u;  // drawOccLate.cs.hlsl:67
+        if (MODE == BLZ_MODE_LATE) {
+            // drawOccLate.cs.hlsl:67, storing only a value that changes
+            const bool wasNonZero = (a.x >> 31) != 0u, wasOne = ((a.x >> 30) & 1u) != 0u;
+            if (visible ? !wasOne : wasNonZero) bv.vis[obj] = visible ? 1u : 0u;
+        }
     }
     const bool emitted = visible && (MODE == BLZ_MODE_LATE ? (a.x >> 31) == 0u : true);  // drawOccLate.cs.hlsl:45
     uint32_t lid = 0u;
@@ -139,15 +143,17 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
     const ViewConsts v = load_view(bv.view);
     uint32_t run = 0, head = 0, tail = 0;
 
-    // frustum stage over OPT slices: obj[k] the object index, ro[k] its render object, vis[k] != 0
-    // when active (LATE: bit 31, with the previous visibility below it)
+    // frustum stage over OPT slices: obj[k] the object index, ro[k] its render object, vis[k] the
+    // object's visibility word (LATE: as read; the object is active when in range) or, in the other
+    // passes, non-zero when the object is active
     float4 ps[OPT], q[OPT], sph[OPT];
     uint2 lod[OPT];
     bool ok[OPT];
-    auto gather = [&](const uint2 (&ro)[OPT], const uint32_t (&vis)[OPT]) {
+    auto active = [&](uint32_t obj, uint32_t vis) -> bool { return MODE == BLZ_MODE_LATE ? obj < limit : vis != 0u; };
+    auto gather = [&](const uint32_t (&obj)[OPT], const uint2 (&ro)[OPT], const uint32_t (&vis)[OPT]) {
 #pragma unroll
         for (int k = 0; k < OPT; ++k) {
-            ok[k] = vis[k] != 0u && ro[k].x < sc.transformCount && ro[k].y < sc.surfaceCount;
+            ok[k] = active(obj[k], vis[k]) && ro[k].x < sc.transformCount && ro[k].y < sc.surfaceCount;
             const uint32_t tid = ok[k] ? ro[k].x : 0u, sid = ok[k] ? ro[k].y : 0u;
             const BlzMeshTransform* tt = sc.transforms;
             if constexpr (!SINGLE) {
@@ -168,18 +174,19 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
     auto test = [&](const uint32_t (&obj)[OPT], const uint32_t (&vis)[OPT]) {
 #pragma unroll
         for (int k = 0; k < OPT; ++k) {
-            const bool act = vis[k] != 0u;
+            const bool act = active(obj[k], vis[k]);
             const bool lodOk = lod[k].x < sc.lodCount && lod[k].y <= sc.lodCount - lod[k].x;
             const bool good = ok[k] && lodOk;
             if (act && !good) flags |= BLZ_FLAG_BAD_INDEX;
             const Vec3 c = view_transform(v.rows, model_to_world(Vec3{sph[k].x, sph[k].y, sph[k].z}, ps[k], q[k]));
             const float r = BLZ_FM(sph[k].w, ps[k].w);
             const bool inFrustum = good && frustum_check(c, r, v);
-            if (MODE == BLZ_MODE_LATE && act && !inFrustum) bv.vis[obj[k]] = 0u;  // drawOccLate.cs.hlsl:67
+            // drawOccLate.cs.hlsl:67, storing only a value that changes
+            if (MODE == BLZ_MODE_LATE && act && !inFrustum && vis[k] != 0u) bv.vis[obj[k]] = 0u;
             const unsigned m = __ballot_sync(0xFFFFFFFFu, inFrustum);
             if (inFrustum) {
                 uint4* e = reinterpret_cast<uint4*>(ring + ((tail + __popc(m & lanemask_lt())) & (kRing - 1u)));
-                const uint32_t tag = (MODE == BLZ_MODE_LATE && (vis[k] & 0x7FFFFFFFu) != 0u) ? 0x80000000u : 0u;
+                const uint32_t tag = MODE != BLZ_MODE_LATE ? 0u : (vis[k] != 0u ? 0x80000000u : 0u) | (vis[k] == 1u ? 0x40000000u : 0u);
                 e[0] = make_uint4(obj[k] | tag, __float_as_uint(c.x), __float_as_uint(c.y), __float_as_uint(c.z));
                 e[1] = make_uint4(__float_as_uint(r), __float_as_uint(ps[k].w), lod[k].x, lod[k].y);
             }
@@ -203,7 +210,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
             nro[k] = in ? __ldg(reinterpret_cast<const uint2*>(bv.objects) + i) : make_uint2(0u, 0u);
             nvis[k] = in ? 1u : 0u;
             if (MODE == BLZ_MODE_FIRST && in) nvis[k] = __ldg(bv.vis + i);
-            if (MODE == BLZ_MODE_LATE && in) nvis[k] = bv.vis[i] | 0x80000000u;  // rewritten later by this warp: coherent load
+            if (MODE == BLZ_MODE_LATE) nvis[k] = in ? bv.vis[i] : 0u;  // rewritten later by this warp: coherent load
         }
     };
     // candidates packed by pass 1, taken STEP at a time (or the rest, at the end)
@@ -223,7 +230,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
         }
         __syncwarp();
         ahead += n;
-        gather(ro, vis);
+        gather(obj, ro, vis);
         test(obj, vis);
     };
 
@@ -234,7 +241,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
 #pragma unroll
         for (int k = 0; k < OPT; ++k) {
             ro[k] = nro[k];
-            vis[k] = nvis[k];  // in range (LATE marks it in bit 31); pass 1: visible last frame (drawOccFirst.cs.hlsl:22-25)
+            vis[k] = nvis[k];  // pass 1: active when visible last frame (drawOccFirst.cs.hlsl:22-25)
             obj[k] = sb + k * 32u + lane;
         }
         if constexpr (PACK) {
@@ -248,7 +255,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
             }
             if (atail - ahead >= STEP) take_candidates(STEP);
         } else {
-            gather(ro, vis);
+            gather(obj, ro, vis);
             if (sb + STEP < limit) prefetch(sb + STEP);
             test(obj, vis);
         }

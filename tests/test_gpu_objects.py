@@ -251,3 +251,22 @@ def test_capture_refuses_to_grow_scratch(culler, c1):
         g = culler.capture_end()
         g.close()
     assert ei.value.code == 2  # BLZ_ERR_CAPACITY
+
+
+def test_late_pass_with_unusual_visibility_words(culler, c1):
+    """Pass 2 treats any non-zero word as 'visible last frame' and rewrites every word to 0 or 1,
+    as drawOccLate.cs.hlsl does, whatever the word held (0, 1, 2, 2^31, 2^32-1)."""
+    v = view_for(zfar=1e4)
+    depth = O.depth_raster(v, S.make_occluders(np.random.default_rng(8), 400), W, H)
+    pyr = DevicePyramid(W, H)
+    culler.generate_depth_pyramid(pyr, torch.from_numpy(depth).cuda())
+    words = np.array([0, 1, 2, 0x80000000, 0xFFFFFFFF], np.uint32)
+    vis0 = words[np.random.default_rng(9).integers(0, len(words), c1.count)]
+    vis = torch.from_numpy(vis0.view(np.int32).copy()).cuda()
+    t = Target.alloc(c1.count)
+    culler.draw_cull_occlusion_pass(v, vis, pyr, t)
+    assert culler.check() == 0
+    ovis = vis0.copy()
+    n, recs, _ = O.cull(2, v, c1, vis=ovis, pyramid=O.pyramid_build(depth))
+    assert_records_equal(t.read(), (n, recs), "late, unusual words")
+    assert np.array_equal(vis.cpu().numpy().view(np.uint32), ovis)
