@@ -113,7 +113,7 @@ void bind_chunk_scratch(blz_ctx* c, PipeParams& p) {
     char* m = static_cast<char*>(c->chunkMem);
     p.staged = reinterpret_cast<uint2*>(m);
     p.chunkCount = reinterpret_cast<uint32_t*>(m + c->chunkObjects * sizeof(uint2));
-    p.workCounter = c->pyrCounter + 1;  // [0] is the pyramid's
+    p.workCounter = c->workCounter;
     p.scratch = c->scratch;
 }
 
@@ -150,8 +150,8 @@ int blz_ctx_create(int device, blz_ctx** out) {
         const unsigned int one = 1u;
         e = cudaMemcpy(static_cast<char*>(c->scratchMem) + 4, &one, sizeof one, cudaMemcpyHostToDevice);
     }
-    if (e == cudaSuccess) e = cudaMalloc(&c->pyrCounter, sizeof(unsigned int) * 4);
-    if (e == cudaSuccess) e = cudaMemset(c->pyrCounter, 0, sizeof(unsigned int) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&c->workCounter, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(c->workCounter, 0, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMallocHost(&c->pinned, kPinnedBytes);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->pinnedDone, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -170,7 +170,7 @@ int blz_ctx_destroy(blz_ctx* c) {
     cudaDeviceSynchronize();
     release_scene(c);
     if (c->scratchMem) cudaFree(c->scratchMem);
-    if (c->pyrCounter) cudaFree(c->pyrCounter);
+    if (c->workCounter) cudaFree(c->workCounter);
     if (c->pinned) cudaFreeHost(c->pinned);
     if (c->pinnedDone) cudaEventDestroy(c->pinnedDone);
     if (c->batchDev) cudaFree(c->batchDev);
@@ -198,7 +198,7 @@ int blz_ctx_check(blz_ctx* c, blz_stream_t stream, uint32_t* flagsOut) {
         // a timed-out launch may have left the ticket mid-way: restart the protocol on a new epoch
         unsigned int fresh[3] = {0u, hdr[1] + 2u, 0u};
         cudaMemcpy(c->scratchMem, fresh, sizeof fresh, cudaMemcpyHostToDevice);
-        cudaMemset(c->pyrCounter, 0, sizeof(unsigned int));
+        cudaMemset(c->workCounter, 0, sizeof(unsigned int));
     }
     if (flagsOut) *flagsOut = flags;
     if (flags & BLZ_FLAG_TIMEOUT) return fail(BLZ_ERR_TIMEOUT, "a device-side wait timed out (flags 0x%x)", flags);
@@ -395,7 +395,6 @@ int blz_pyramid_build(blz_ctx* c, const BlzPyramid* p, const float* depth, blz_s
     bp.mipCount = p->mipCount;
     bp.mode = p->mode;
     for (uint32_t i = 0; i < BLZ_PYRAMID_MAX_MIPS; ++i) bp.mipOffset[i] = p->mipOffset[i];
-    bp.counter = c->pyrCounter;
     uint32_t launches = 0;
     cudaError_t e = launch_pyramid_build(bp, reinterpret_cast<cudaStream_t>(stream), &launches);
     if (e != cudaSuccess) return cuda_fail(e, "pyramid launch");

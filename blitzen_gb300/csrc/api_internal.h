@@ -24,7 +24,7 @@ struct blz_ctx {
     void* scratchMem = nullptr;        // Scratch header + tile states
     blz::Scratch* scratch = nullptr;
     size_t stateCapacity = 0;
-    unsigned int* pyrCounter = nullptr;
+    unsigned int* workCounter = nullptr;  // batch decide launches: next chunk (zero between launches)
     void* pinned = nullptr;            // pinned host staging
     cudaEvent_t pinnedDone = nullptr;  // last copy out of `pinned` has completed
     void* batchDev = nullptr;          // device BatchViewDev[] + tileStart[]

@@ -146,7 +146,6 @@ struct PyramidBuildParams {
     float* data;
     uint32_t width, height, mipCount, mode;
     uint32_t mipOffset[BLZ_PYRAMID_MAX_MIPS];
-    unsigned int* counter;   // scratch: blocks finished
 };
 
 // Launches a kernel with programmatic stream serialization: it may be scheduled while the kernel
