@@ -29,8 +29,10 @@ CLUSTER = np.dtype({
     "offsets": [0, 12, 16, 19, 20, 24, 25],
     "itemsize": 32,
 })
+INDIRECT_TASK = np.dtype([("taskId", "<u4"), ("groupCountX", "<u4"), ("groupCountY", "<u4"), ("groupCountZ", "<u4")])
+MESH_TASK_PAYLOAD = np.dtype([("drawId", "<u4"), ("meshletIndices", "<u4", 32)])
 for _dt, _n in ((RENDER_OBJECT, 8), (MESH_TRANSFORM, 32), (PRIMITIVE_SURFACE, 32), (LOD_DATA, 32),
-                (LOD_INSTANCE_COUNTER, 8), (CLUSTER, 32)):
+                (LOD_INSTANCE_COUNTER, 8), (CLUSTER, 32), (INDIRECT_TASK, 16), (MESH_TASK_PAYLOAD, 132)):
     assert _dt.itemsize == _n
 
 STRIDE_VULKAN = 24
@@ -40,6 +42,7 @@ HIZ_VULKAN = 1
 MODE_FRUSTUM, MODE_FIRST, MODE_LATE, MODE_TEMPORAL = 0, 1, 2, 3
 SCENE_COPY_FROM_HOST, SCENE_BORROW_DEVICE = 0, 1
 NOALLOC_MAX_OBJECTS = 1 << 20
+NO_MESHLET = 0xFFFFFFFF
 
 FLAG_COMMAND_OVERFLOW = 1
 FLAG_INSTANCE_OVERFLOW = 2
@@ -99,6 +102,11 @@ class CullTarget(C.Structure):
                 ("drawCount", C.c_void_p)]
 
 
+class TaskTarget(C.Structure):
+    _fields_ = [("tasks", C.c_void_p), ("payloads", C.c_void_p), ("taskCapacity", C.c_uint32),
+                ("payloadCapacity", C.c_uint32), ("taskCount", C.c_void_p), ("payloadCount", C.c_void_p)]
+
+
 class BatchView(C.Structure):
     _fields_ = [("view", CameraViewData), ("list", RenderList), ("mode", C.c_uint32),
                 ("reserved0", C.c_uint32), ("visibility", C.c_void_p), ("pyramid", C.POINTER(Pyramid)),
@@ -137,11 +145,11 @@ class ServeStats(C.Structure):
 # Sizes of the C structs (checked against a compiled probe in the tests).
 C_SIZES = {"BlzBatchView": 512, "BlzServeRequest": 512, "BlzServeResult": 40, "BlzServeStats": 80,
            "BlzServeConfig": 24, "BlzPyramid": 96, "BlzSceneDesc": 80, "BlzCullTarget": 24, "BlzRenderList": 16,
-           "BlzLaunchShape": 16, "BlzCameraViewData": 256}
+           "BlzLaunchShape": 16, "BlzCameraViewData": 256, "BlzTaskTarget": 40}
 CTYPES_OF = {"BlzBatchView": BatchView, "BlzServeRequest": ServeRequest, "BlzServeResult": ServeResult,
              "BlzServeStats": ServeStats, "BlzServeConfig": ServeConfig, "BlzPyramid": Pyramid,
              "BlzSceneDesc": SceneDesc, "BlzCullTarget": CullTarget, "BlzRenderList": RenderList,
-             "BlzLaunchShape": LaunchShape, "BlzCameraViewData": CameraViewData}
+             "BlzLaunchShape": LaunchShape, "BlzCameraViewData": CameraViewData, "BlzTaskTarget": TaskTarget}
 for _name, _cls in CTYPES_OF.items():
     assert C.sizeof(_cls) == C_SIZES[_name], (_name, C.sizeof(_cls))
 
@@ -172,6 +180,7 @@ _PROTOS = {
     "blz_cull_temporal": (_I, [_P, C.POINTER(CameraViewData), RenderList, C.POINTER(Pyramid), C.POINTER(CullTarget), _P]),
     "blz_cull_instanced": (_I, [_P, C.POINTER(CameraViewData), RenderList, _P, _P, _U32, _U32, C.POINTER(CullTarget), _P]),
     "blz_cull_clusters": (_I, [_P, C.POINTER(CameraViewData), RenderList, C.POINTER(Pyramid), C.POINTER(CullTarget), _P, _P]),
+    "blz_cull_cluster_tasks": (_I, [_P, C.POINTER(CameraViewData), RenderList, C.POINTER(Pyramid), C.POINTER(TaskTarget), _P]),
     "blz_cull_batch": (_I, [_P, C.POINTER(BatchView), _U32, _P]),
     "blz_cull_batch_per_view": (_I, [_P, C.POINTER(BatchView), _U32, _P]),
     "blz_batch_graph_create": (_I, [_P, C.POINTER(BatchView), _U32, _P, C.POINTER(_P)]),

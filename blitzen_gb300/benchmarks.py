@@ -26,7 +26,7 @@ import torch
 from . import abi
 from . import scenes as S
 from .abi import BatchView, RenderList
-from .culler import DevicePyramid, Target, to_device
+from .culler import DevicePyramid, Target, TaskTarget, to_device
 
 W, H = 1920, 1080
 
@@ -271,10 +271,18 @@ def clusters(device, reps=30) -> dict:
         c.check(side)
         n = int(t.read()[0])
         nbytes = sc.count * (8 + 32) + sc.clusters.nbytes + n * (abi.STRIDE_VULKAN + 4)
+        # the mesh-shader form of the same cull: one task per object, payloads of 32 meshlets
+        tt = TaskTarget.alloc(sc.count, (cap + 31) // 32 + sc.count)
+        ms_t = _replay_ms(c, lambda: c.cluster_task_cull(v, tt, pyramid=pyr), reps, flush, side)
+        c.check(side)
+        nt, npl = (int(x) for x in tt.read()[:2])
+        tbytes = sc.count * (8 + 32) + sc.clusters.nbytes + nt * 16 + npl * 132
         return {"objects": sc.count, "clusters_in_scene": len(sc.clusters), "cluster_upper_bound": cap,
                 "clusters_emitted": n, "ms": ms, "objects_per_s": sc.count / (ms * 1e-3),
                 "cluster_candidates_per_s": cap / (ms * 1e-3), "algorithmic_bytes": nbytes,
-                "GB/s": nbytes / (ms * 1e-3) / 1e9}
+                "GB/s": nbytes / (ms * 1e-3) / 1e9,
+                "task_form": {"ms": ms_t, "tasks": nt, "payloads": npl, "algorithmic_bytes": tbytes,
+                              "cluster_candidates_per_s": cap / (ms_t * 1e-3)}}
     finally:
         c.close()
 

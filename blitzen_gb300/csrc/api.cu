@@ -3,6 +3,7 @@
 // Host-side counterpart of the reference's cull dispatch code: the renderer members and static
 // dispatch helpers of src/Renderer/BlitzenVulkan/vulkanDraw.cpp:107-622 and
 // src/Renderer/BlitzenDX12/dx12Draw.cpp:114-415, without the graphics API around them.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -109,6 +110,39 @@ int ensure_chunk_scratch(blz_ctx* c, size_t chunks, size_t chunkSize) {
     return BLZ_OK;
 }
 
+// Cluster-cull scratch for `tiles` tiles: tile counts (uint2), object ranges (uint2) and survivor
+// counts per object, then the visibility bits (bitWords per tile). Grown on demand like the
+// object-cull scratch.
+int bind_cluster_scratch(blz_ctx* c, uint32_t tiles, ClusterParams& p) {
+    const size_t objs = static_cast<size_t>(tiles) * cluster_tile_objects();
+    const uint32_t bitWords = std::max<uint32_t>(c->lodClusterMax, 1u);  // 32 objects x max clusters / 32 bits
+    const size_t countBytes = (static_cast<size_t>(tiles) * sizeof(uint2) + 255) & ~size_t(255);
+    const size_t infoBytes = (objs * sizeof(uint2) + 255) & ~size_t(255);
+    const size_t survBytes = (objs * sizeof(uint32_t) + 255) & ~size_t(255);
+    const size_t bitBytes = static_cast<size_t>(tiles) * bitWords * sizeof(uint32_t);
+    const size_t need = countBytes + infoBytes + survBytes + bitBytes;
+    if (need > c->clusterBytes) {
+        if (c->capturing) return fail(BLZ_ERR_CAPACITY, "scratch must grow, which a capture cannot record: run the call once before capturing");
+        if (c->clusterMem) {
+            cudaDeviceSynchronize();
+            cudaFree(c->clusterMem);
+            c->clusterMem = nullptr;
+            c->clusterBytes = 0;
+        }
+        const size_t want = need + need / 4;
+        if (cudaMalloc(&c->clusterMem, want) != cudaSuccess)
+            return fail(BLZ_ERR_OUT_OF_MEMORY, "cluster-cull scratch of %zu bytes", want);
+        c->clusterBytes = want;
+    }
+    char* m = static_cast<char*>(c->clusterMem);
+    p.tileCount = reinterpret_cast<uint32_t*>(m);
+    p.objInfo = reinterpret_cast<uint2*>(m + countBytes);
+    p.objSurv = reinterpret_cast<uint32_t*>(m + countBytes + infoBytes);
+    p.bits = reinterpret_cast<uint32_t*>(m + countBytes + infoBytes + survBytes);
+    p.bitWords = bitWords;
+    return BLZ_OK;
+}
+
 void bind_chunk_scratch(blz_ctx* c, PipeParams& p) {
     char* m = static_cast<char*>(c->chunkMem);
     p.staged = reinterpret_cast<uint2*>(m);
@@ -176,6 +210,7 @@ int blz_ctx_destroy(blz_ctx* c) {
     if (c->batchDev) cudaFree(c->batchDev);
     if (c->chunkMem) cudaFree(c->chunkMem);
     if (c->instScratch) cudaFree(c->instScratch);
+    if (c->clusterMem) cudaFree(c->clusterMem);
     delete c;
     return BLZ_OK;
 }
@@ -259,6 +294,18 @@ int blz_scene_upload(blz_ctx* c, const BlzSceneDesc* s, uint32_t flags, blz_stre
         return fail(BLZ_ERR_INVALID_ARGUMENT,
                     "scene tables must be aligned: transforms 32 bytes, surfaces/LODs/clusters 16, render objects 8");
     }
+    // the largest cluster range a LOD can select bounds the candidates of a tile of objects
+    uint32_t lodClusterMax = 0;
+    if (s->lodCount) {
+        std::vector<BlzLodData> lods(s->lodCount);
+        cudaError_t e = cudaMemcpy(lods.data(), s->lods, sizeof(BlzLodData) * lods.size(), cudaMemcpyDefault);
+        if (e != cudaSuccess) {
+            release_scene(c);
+            return cuda_fail(e, "reading the LOD table");
+        }
+        for (const BlzLodData& l : lods) lodClusterMax = std::max(lodClusterMax, std::min(l.clusterCount, s->clusterCount));
+    }
+    c->lodClusterMax = lodClusterMax;
     c->scene = t;
     c->defaultObjects = t.objects;
     c->defaultCount = s->renderObjectCount;
@@ -589,9 +636,9 @@ int blz_cull_clusters(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList l
     if (!c->scene.clusters && c->scene.clusterCount) return fail(BLZ_ERR_INVALID_ARGUMENT, "scene has no cluster table");
     uint32_t tiles = (count + cluster_tile_objects() - 1) / cluster_tile_objects();
     if (tiles == 0) tiles = 1;
-    rc = ensure_chunk_scratch(c, tiles, 1);  // one count per tile
-    if (rc != BLZ_OK) return rc;
     ClusterParams p{};
+    rc = bind_cluster_scratch(c, tiles, p);
+    if (rc != BLZ_OK) return rc;
     p.sc = c->scene;
     p.objects = objs;
     p.count = count;
@@ -603,13 +650,48 @@ int blz_cull_clusters(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList l
     p.clusterIds = clusterIds;
     p.drawCount = target->drawCount;
     p.scratch = c->scratch;
-    {
-        PipeParams scratch{};
-        bind_chunk_scratch(c, scratch);
-        p.tileCount = scratch.chunkCount;
-    }
     cudaError_t e = launch_cluster_cull(p, *view, reinterpret_cast<cudaStream_t>(s));
     if (e != cudaSuccess) return cuda_fail(e, "cluster cull launch");
+    c->launches += 2;  // count, write
+    return BLZ_OK;
+}
+
+int blz_cull_cluster_tasks(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, const BlzPyramid* pyr,
+                           const BlzTaskTarget* target, blz_stream_t s) {
+    if (!c || !view) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or view is NULL");
+    if (!target) return fail(BLZ_ERR_INVALID_ARGUMENT, "target is NULL");
+    if (!target->taskCount || !target->payloadCount)
+        return fail(BLZ_ERR_INVALID_ARGUMENT, "target taskCount or payloadCount is NULL");
+    if ((target->taskCapacity > 0 && !target->tasks) || (target->payloadCapacity > 0 && !target->payloads))
+        return fail(BLZ_ERR_INVALID_ARGUMENT, "target tasks or payloads is NULL");
+    if (reinterpret_cast<uintptr_t>(target->tasks) % 4 != 0 || reinterpret_cast<uintptr_t>(target->payloads) % 4 != 0)
+        return fail(BLZ_ERR_INVALID_ARGUMENT, "target tasks and payloads must be 4-byte aligned");
+    const BlzRenderObject* objs = nullptr;
+    uint32_t count = 0;
+    int rc = resolve_list(c, list, &objs, &count);
+    if (rc != BLZ_OK) return rc;
+    rc = check_pyramid(pyr, false);
+    if (rc != BLZ_OK) return rc;
+    if (!c->scene.clusters && c->scene.clusterCount) return fail(BLZ_ERR_INVALID_ARGUMENT, "scene has no cluster table");
+    uint32_t tiles = (count + cluster_tile_objects() - 1) / cluster_tile_objects();
+    if (tiles == 0) tiles = 1;
+    ClusterParams p{};
+    rc = bind_cluster_scratch(c, tiles, p);
+    if (rc != BLZ_OK) return rc;
+    p.sc = c->scene;
+    p.objects = objs;
+    p.count = count;
+    p.pyr = pyramid_view(pyr);
+    p.hasPyramid = pyr ? 1u : 0u;
+    p.scratch = c->scratch;
+    p.tasks = reinterpret_cast<uint32_t*>(target->tasks);
+    p.payloads = reinterpret_cast<uint32_t*>(target->payloads);
+    p.taskCapacity = target->taskCapacity;
+    p.payloadCapacity = target->payloadCapacity;
+    p.taskCount = target->taskCount;
+    p.payloadCount = target->payloadCount;
+    cudaError_t e = launch_cluster_tasks(p, *view, reinterpret_cast<cudaStream_t>(s));
+    if (e != cudaSuccess) return cuda_fail(e, "cluster task cull launch");
     c->launches += 2;  // count, write
     return BLZ_OK;
 }

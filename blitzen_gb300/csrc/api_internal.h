@@ -34,6 +34,9 @@ struct blz_ctx {
     size_t chunkSlots = 0;             // chunk count capacity
     uint32_t* instScratch = nullptr;   // instanced cull: group x LOD counts, then LOD totals
     size_t instWords = 0;
+    void* clusterMem = nullptr;        // cluster cull: tile counts, object ranges and survivors, visibility bits
+    size_t clusterBytes = 0;
+    uint32_t lodClusterMax = 0;        // largest clusterCount of the scene's LODs (clamped to the cluster table)
     bool hasScene = false;
     blz::SceneT scene{};
     const BlzRenderObject* defaultObjects = nullptr;

@@ -1,17 +1,22 @@
-// cull_clusters.cu — object pass, cluster expansion and per-cluster culling in one launch.
+// cull_clusters.cu — object pass, cluster expansion and per-cluster culling.
 //
 // The reference splits this into PreClusterDrawCull.comp.glsl:13-47 (object frustum + LOD, then a
 // serial loop that materialises one 12-byte ClusterDispatchData per cluster), a fence wait and CPU
 // read-back of the cluster count (src/Renderer/BlitzenVulkan/vulkanDraw.cpp:874-905), and
 // InitialClusterCull.comp.glsl:12-55 (one draw per cluster, its cone test commented out). Here a
-// block takes a tile of objects, decides them and prefix-sums their cluster counts in shared
+// block takes a tile of 32 objects, decides them and prefix-sums their cluster counts in shared
 // memory, then walks the tile's clusters in order (a binary search maps a cluster slot back to
 // its object), testing each one: sphere frustum, Hi-Z when a pyramid is bound, and the normal cone
 // in meshoptimizer's documented form (VendorCode/Meshoptimizer/meshoptimizer.h:561-569).
-// Two launches, no block waiting on another: the count launch writes each tile's number of
-// surviving clusters; the write launch sums the counts of the tiles before its own (a strided
-// read), repeats the same tests and writes the records at their final slots. Nothing is
-// materialised and the host never waits.
+// Two launches, no block waiting on another. The test launch keeps one visibility bit per
+// candidate cluster, each object's cluster range and the tile's survivor count; the emit launch
+// sums the counts of the tiles before its own (a strided read) and writes a record for every set
+// bit at its final position, without repeating a test. Nothing is materialised per candidate but
+// the bit, and the host never waits.
+//
+// The task form (mesh-shader consumers) runs the same tests; its test launch also keeps each
+// object's number of survivors, from which the emit launch places the object's task record and
+// its run of 32-meshlet payloads (MeshTaskPayload, VulkanShaderHeaders/ShaderBuffers.glsl:203-206).
 #include "blz_device.cuh"
 #include "kernels.h"
 
@@ -31,11 +36,10 @@ struct ClusterObj {
 // Sphere, Hi-Z and cone tests of one cluster of an object. snorm[i] holds (float)(i - 128) / 127,
 // divided once per block: the int8 cone axis and cutoff take only those 256 values.
 __device__ __forceinline__ bool cluster_visible(const ClusterParams& p, const ViewConsts& v, const ClusterObj& o,
-                                                uint32_t cid, const float* snorm, uint32_t& indexCount,
-                                                uint32_t& dataOffset) {
+                                                uint32_t cid, const float* snorm) {
     const float4* cp = reinterpret_cast<const float4*>(p.sc.clusters + cid);
     const float4 sph = __ldg(cp);
-    const uint4 meta = __ldg(reinterpret_cast<const uint4*>(cp + 1));  // cone s8x4, dataOffset, counts, pad
+    const uint32_t cone = __ldg(reinterpret_cast<const uint32_t*>(cp + 1));  // int8 axis xyz, cutoff
     const Vec3 w = model_to_world(Vec3{sph.x, sph.y, sph.z}, o.posScale, o.quat);
     const Vec3 c = view_transform(v.rows, w);
     const float r = BLZ_FM(sph.w, o.posScale.w);
@@ -45,8 +49,8 @@ __device__ __forceinline__ bool cluster_visible(const ClusterParams& p, const Vi
         if (project_sphere(c, r, v.zNear, v.proj0, v.proj5, aabb)) vis = vis && occlusion(aabb, p.pyr, v, c, r);
     }
     if (vis) {
-        const int ax = static_cast<int8_t>(meta.x & 0xFFu), ay = static_cast<int8_t>((meta.x >> 8) & 0xFFu);
-        const int az = static_cast<int8_t>((meta.x >> 16) & 0xFFu), ac = static_cast<int8_t>(meta.x >> 24);
+        const int ax = static_cast<int8_t>(cone & 0xFFu), ay = static_cast<int8_t>((cone >> 8) & 0xFFu);
+        const int az = static_cast<int8_t>((cone >> 16) & 0xFFu), ac = static_cast<int8_t>(cone >> 24);
         const Vec3 axm{snorm[ax + 128], snorm[ay + 128], snorm[az + 128]};
         const float cutoff = snorm[ac + 128];
         const Vec3 axis = rotate_quat(axm, o.quat);
@@ -56,32 +60,45 @@ __device__ __forceinline__ bool cluster_visible(const ClusterParams& p, const Vi
         const float dp = BLZ_FA(BLZ_FA(BLZ_FM(nx, axis.x), BLZ_FM(ny, axis.y)), BLZ_FM(nz, axis.z));
         if (dp >= cutoff) vis = false;
     }
-    dataOffset = meta.y;
-    indexCount = ((meta.z >> 8) & 0xFFu) * 3u;  // triangleCount * 3
     return vis;
 }
 
-template <bool WRITE>
-__global__ void __launch_bounds__(kClThreads) cull_clusters_kernel(const ClusterParams p, const BlzCameraViewData view) {
+// Last object of the tile whose first slot is <= slot.
+__device__ __forceinline__ uint32_t slot_object(const uint32_t* s_start, uint32_t slot) {
+    uint32_t lo = 0, hi = kClObjects;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_start[mid] <= slot) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Test launch: object pass, expansion over the chosen LODs' clusters and the cluster tests. Keeps
+// for the emit launch each object's cluster range (objInfo), one visibility bit per candidate
+// (bits: the tile's slots in order, bitWords words per tile) and the tile's survivor count
+// (task form: per-object survivors, and the tile's {tasks, payloads}).
+template <bool TASKS>
+__global__ void __launch_bounds__(kClThreads) cluster_test_kernel(const ClusterParams p, const BlzCameraViewData view) {
+    static_assert(kClObjects == 32, "the tile's objects are one warp");
     __shared__ ClusterObj s_obj[kClObjects];
     __shared__ uint32_t s_start[kClObjects + 1];
     __shared__ uint32_t s_warp[kClWarps];
-    __shared__ uint32_t s_base;
+    __shared__ uint32_t s_surv[kClObjects];
     __shared__ unsigned int s_flags;
     __shared__ float s_snorm[256];
     if (threadIdx.x == 0) s_flags = 0u;
     for (uint32_t i = threadIdx.x; i < 256u; i += kClThreads)
         s_snorm[i] = BLZ_FD(static_cast<float>(static_cast<int>(i) - 128), 127.0f);
-    __syncthreads();
     const uint32_t tile = blockIdx.x;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const ViewConsts v = load_view(view);
 
     // object pass: PreClusterDrawCull.comp.glsl:20-37
-    uint32_t count = 0;
-    unsigned int flags = 0u;
-    if (threadIdx.x < kClObjects) {
-        const uint32_t i = tile * kClObjects + threadIdx.x;
+    if (warp == 0) {
+        const ViewConsts v = load_view(view);
+        const uint32_t i = tile * kClObjects + lane;
+        uint32_t count = 0;
+        unsigned int flags = 0u;
         ClusterObj o;
         o.objectId = i;
         o.clusterOffset = 0;
@@ -122,112 +139,223 @@ __global__ void __launch_bounds__(kClThreads) cull_clusters_kernel(const Cluster
                 }
             }
         }
-        s_obj[threadIdx.x] = o;
-    }
-    if (flags) atomicOr(&s_flags, flags);
-    // exclusive scan of the per-object cluster counts (the first kClObjects / 32 warps hold them)
-    constexpr uint32_t kObjWarps = kClObjects / 32;
-    static_assert(kClObjects % 32 == 0 && kObjWarps >= 1 && kObjWarps <= 2, "one or two warps of objects");
-    if (warp < kObjWarps) {
+        // exclusive scan of the per-object cluster counts
         uint32_t incl = count;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= static_cast<uint32_t>(o)) incl += n;
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= static_cast<uint32_t>(d)) incl += n;
         }
-        if (lane == 31) s_warp[warp] = incl;
-        s_start[threadIdx.x] = incl - count;  // provisional (warp-local)
+        if (__shfl_sync(0xFFFFFFFFu, incl, 31) > 32u * p.bitWords) {
+            // a LOD's cluster range grew past the largest one the scene had at upload: the tile's
+            // bits would not fit, so it emits nothing and flags the scene
+            flags |= BLZ_FLAG_BAD_INDEX;
+            count = 0u;
+            incl = 0u;
+        }
+        s_obj[lane] = o;
+        s_surv[lane] = 0u;
+        p.objInfo[tile * kClObjects + lane] = make_uint2(o.clusterOffset, count);
+        s_start[lane] = incl - count;
+        if (lane == 31) s_start[kClObjects] = incl;
+        flags = __reduce_or_sync(0xFFFFFFFFu, flags);
+        if (lane == 0) s_flags = flags;
     }
     __syncthreads();
-    if (threadIdx.x >= 32 && threadIdx.x < kClObjects) s_start[threadIdx.x] += s_warp[0];
-    if (threadIdx.x == 0) s_start[kClObjects] = kObjWarps == 2 ? s_warp[0] + s_warp[1] : s_warp[0];
+    const uint32_t T = s_start[kClObjects];
+    const ViewConsts v = load_view(view);
+    uint32_t* bits = p.bits + static_cast<size_t>(tile) * p.bitWords;
+    const uint32_t lt = lanemask_lt();
+    uint32_t survivors = 0;
+    for (uint32_t chunk = 0; chunk < T; chunk += kClThreads) {
+        const uint32_t slot = chunk + threadIdx.x;
+        bool vis = false;
+        uint32_t lo = 0;
+        if (slot < T) {
+            lo = slot_object(s_start, slot);
+            vis = cluster_visible(p, v, s_obj[lo], s_obj[lo].clusterOffset + (slot - s_start[lo]), s_snorm);
+        }
+        const unsigned bal = __ballot_sync(0xFFFFFFFFu, vis);
+        if (lane == 0 && chunk + 32u * warp < T) bits[(chunk >> 5) + warp] = bal;
+        if constexpr (TASKS) {
+            // lanes of one object add once
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, vis ? lo : 0x100u + lane);
+            if (vis && (peers & lt) == 0u) atomicAdd(&s_surv[lo], static_cast<uint32_t>(__popc(peers)));
+        } else {
+            survivors += __popc(bal);
+        }
+    }
+    if constexpr (!TASKS) {
+        if (lane == 0) s_warp[warp] = survivors;
+    }
+    __syncthreads();
+    if constexpr (TASKS) {
+        if (warp == 0) {
+            const uint32_t sv = s_surv[lane];
+            p.objSurv[tile * kClObjects + lane] = sv;
+            const uint32_t tasks = __popc(__ballot_sync(0xFFFFFFFFu, sv != 0u));
+            const uint32_t payloads = __reduce_add_sync(0xFFFFFFFFu, (sv + 31u) >> 5);
+            if (lane == 0) reinterpret_cast<uint2*>(p.tileCount)[tile] = make_uint2(tasks, payloads);
+        }
+    } else if (threadIdx.x == 0) {
+        uint32_t total = 0;
+        for (int w = 0; w < kClWarps; ++w) total += s_warp[w];
+        p.tileCount[tile] = total;
+    }
+    if (threadIdx.x == 0 && s_flags) atomicOr(&p.scratch->status, s_flags);
+}
+
+// Emit launch: no test is repeated. The tile's cluster ranges and visibility bits come from the
+// test launch; the records (task form: tasks and payloads) of the tiles before this one are summed
+// from their counts, and each set bit is written at its final position in slot order.
+template <bool TASKS>
+__global__ void __launch_bounds__(kClThreads) cluster_emit_kernel(const ClusterParams p) {
+    __shared__ uint32_t s_start[kClObjects + 1];
+    __shared__ uint32_t s_off[kClObjects];
+    __shared__ uint32_t s_first[kClObjects];  // task form: the object's first payload
+    __shared__ uint32_t s_rank[kClObjects];   // task form: survivors of the tile before the object
+    __shared__ uint32_t s_warp[kClWarps];
+    __shared__ uint32_t s_warp2[kClWarps];
+    __shared__ uint32_t s_base;
+    const uint32_t tile = blockIdx.x;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t lt = lanemask_lt();
+
+    // the records (task form: tasks, payloads) of the tiles before this one
+    uint32_t before = 0, before2 = 0;
+    if constexpr (TASKS) {
+        const uint2* tc = reinterpret_cast<const uint2*>(p.tileCount);
+        for (uint32_t t = threadIdx.x; t < tile; t += kClThreads) {
+            const uint2 c = __ldcg(tc + t);
+            before += c.x;
+            before2 += c.y;
+        }
+        before2 = __reduce_add_sync(0xFFFFFFFFu, before2);
+    } else {
+        for (uint32_t t = threadIdx.x; t < tile; t += kClThreads) before += __ldcg(p.tileCount + t);
+    }
+    before = __reduce_add_sync(0xFFFFFFFFu, before);
+    if (lane == 0) {
+        s_warp[warp] = before;
+        s_warp2[warp] = before2;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t base = 0, baseP = 0;
+#pragma unroll
+        for (int w = 0; w < kClWarps; ++w) {
+            base += s_warp[w];
+            baseP += s_warp2[w];
+        }
+        const uint2 info = __ldcg(p.objInfo + tile * kClObjects + lane);  // {clusterOffset, count}
+        uint32_t incl = info.y;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= static_cast<uint32_t>(d)) incl += n;
+        }
+        s_start[lane] = incl - info.y;
+        s_off[lane] = info.x;
+        if (lane == 31) s_start[kClObjects] = incl;
+        if constexpr (TASKS) {
+            // per object: its task slot, first payload and the tile's survivors before it
+            const uint32_t sv = __ldcg(p.objSurv + tile * kClObjects + lane);
+            const uint32_t k = (sv + 31u) >> 5;
+            uint32_t is = sv, ik = k;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, is, d);
+                const uint32_t b = __shfl_up_sync(0xFFFFFFFFu, ik, d);
+                if (lane >= static_cast<uint32_t>(d)) {
+                    is += a;
+                    ik += b;
+                }
+            }
+            const unsigned has = __ballot_sync(0xFFFFFFFFu, sv != 0u);
+            const uint32_t first = baseP + ik - k;
+            s_rank[lane] = is - sv;
+            s_first[lane] = first;
+            if (sv != 0u) {
+                const uint32_t t = base + __popc(has & lt);
+                if (t < p.taskCapacity) {
+                    uint32_t* tw = p.tasks + static_cast<size_t>(t) * 4u;
+                    tw[0] = first;
+                    tw[1] = k;
+                    tw[2] = 1u;
+                    tw[3] = 1u;
+                }
+                const uint32_t tail = sv & 31u;  // the last payload's unused slots
+                const uint32_t last = first + k - 1u;
+                if (tail != 0u && last < p.payloadCapacity) {
+                    uint32_t* pw = p.payloads + static_cast<size_t>(last) * 33u + 1u;
+                    for (uint32_t e = tail; e < 32u; ++e) pw[e] = BLZ_NO_MESHLET;
+                }
+            }
+            if (lane == 31 && tile == gridDim.x - 1u) {
+                const uint32_t nt = base + __popc(has), np = baseP + ik;
+                *p.taskCount = nt;
+                *p.payloadCount = np;
+                if (nt > p.taskCapacity || np > p.payloadCapacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
+            }
+        } else if (lane == 0) {
+            s_base = base;
+        }
+    }
     __syncthreads();
     const uint32_t T = s_start[kClObjects];
-
-    if constexpr (!WRITE) {
-        // count the surviving clusters of the tile
-        uint32_t survivors = 0;
-        for (uint32_t slot = threadIdx.x; slot < T; slot += kClThreads) {
-            uint32_t lo = 0, hi = kClObjects;  // last object with start <= slot
-            while (hi - lo > 1u) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (s_start[mid] <= slot) lo = mid;
-                else hi = mid;
-            }
-            uint32_t ic, doff;
-            if (cluster_visible(p, v, s_obj[lo], s_obj[lo].clusterOffset + (slot - s_start[lo]), s_snorm, ic, doff)) ++survivors;
-        }
+    const uint32_t words = (T + 31u) >> 5;
+    const uint32_t* bits = p.bits + static_cast<size_t>(tile) * p.bitWords;
+    uint32_t run = TASKS ? 0u : s_base;  // records before the current round of words
+    for (uint32_t w0 = 0; w0 < words; w0 += kClThreads) {
+        const uint32_t w = w0 + threadIdx.x;
+        uint32_t b = w < words ? __ldcg(bits + w) : 0u;
+        const uint32_t c = __popc(b);
+        uint32_t incl = c;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) survivors += __shfl_xor_sync(0xFFFFFFFFu, survivors, o);
-        __syncthreads();  // every s_warp read of the scan above is done
-        if (lane == 0) s_warp[warp] = survivors;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t total = 0;
-            for (int w = 0; w < kClWarps; ++w) total += s_warp[w];
-            p.tileCount[tile] = total;
-            if (s_flags) atomicOr(&p.scratch->status, s_flags);
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= static_cast<uint32_t>(d)) incl += n;
         }
-    } else {
-        // the records of the tiles before this one
-        uint32_t before = 0;
-        for (uint32_t t = threadIdx.x; t < tile; t += kClThreads) before += __ldcg(p.tileCount + t);
+        if (w0 != 0) __syncthreads();  // the previous round's s_warp reads are done
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        uint32_t q = run + incl - c, total = 0;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xFFFFFFFFu, before, o);
-        __syncthreads();  // every s_warp read of the scan above is done
-        if (lane == 0) s_warp[warp] = before;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t b = 0;
-            for (int w = 0; w < kClWarps; ++w) b += s_warp[w];
-            s_base = b;
+        for (int ww = 0; ww < kClWarps; ++ww) {
+            const uint32_t n = s_warp[ww];
+            if (ww < static_cast<int>(warp)) q += n;
+            total += n;
         }
-        __syncthreads();
-
-        // the tile's clusters in slot order, records at their final positions
-        uint32_t run = s_base;
-        const uint32_t lt = lanemask_lt();
-        for (uint32_t chunk = 0; chunk < T; chunk += kClThreads) {
-            const uint32_t slot = chunk + threadIdx.x;
-            bool vis = false;
-            uint32_t ic = 0, doff = 0, cid = 0, obj = 0;
-            if (slot < T) {
-                uint32_t lo = 0, hi = kClObjects;
-                while (hi - lo > 1u) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (s_start[mid] <= slot) lo = mid;
-                    else hi = mid;
+        while (b != 0u) {
+            const uint32_t slot = w * 32u + static_cast<uint32_t>(__ffs(b) - 1);
+            b &= b - 1u;
+            const uint32_t lo = slot_object(s_start, slot);
+            const uint32_t cid = s_off[lo] + (slot - s_start[lo]);
+            if constexpr (TASKS) {
+                const uint32_t rank = q - s_rank[lo];
+                const uint32_t pi = s_first[lo] + (rank >> 5);
+                if (pi < p.payloadCapacity) {
+                    uint32_t* pw = p.payloads + static_cast<size_t>(pi) * 33u;
+                    pw[1u + (rank & 31u)] = cid;
+                    if ((rank & 31u) == 0u) pw[0] = tile * kClObjects + lo;
                 }
-                cid = s_obj[lo].clusterOffset + (slot - s_start[lo]);
-                obj = s_obj[lo].objectId;
-                vis = cluster_visible(p, v, s_obj[lo], cid, s_snorm, ic, doff);
+            } else if (q < p.capacity) {
+                // InitialClusterCull.comp.glsl:48-54: {objectId, triangleCount * 3, 1, dataOffset, 0, 0}
+                const uint4 meta = __ldg(reinterpret_cast<const uint4*>(p.sc.clusters + cid) + 1);
+                uint32_t* rec = reinterpret_cast<uint32_t*>(p.cmds + static_cast<size_t>(q) * p.stride);
+                rec[0] = tile * kClObjects + lo;
+                rec[1] = ((meta.z >> 8) & 0xFFu) * 3u;
+                rec[2] = 1u;
+                rec[3] = meta.y;
+                rec[4] = 0u;
+                rec[5] = 0u;
+                if (p.clusterIds) p.clusterIds[q] = cid;
             }
-            const unsigned b = __ballot_sync(0xFFFFFFFFu, vis);
-            __syncthreads();  // the previous chunk's s_warp reads are done
-            if (lane == 0) s_warp[warp] = __popc(b);
-            __syncthreads();
-            uint32_t beforeW = 0, chunkTotal = 0;
-#pragma unroll
-            for (int w = 0; w < kClWarps; ++w) {
-                const uint32_t c = s_warp[w];
-                if (w < static_cast<int>(warp)) beforeW += c;
-                chunkTotal += c;
-            }
-            if (vis) {
-                const uint32_t out = run + beforeW + __popc(b & lt);
-                if (out < p.capacity) {
-                    uint32_t* rec = reinterpret_cast<uint32_t*>(p.cmds + static_cast<size_t>(out) * p.stride);
-                    rec[0] = obj;
-                    rec[1] = ic;
-                    rec[2] = 1u;
-                    rec[3] = doff;
-                    rec[4] = 0u;
-                    rec[5] = 0u;
-                    if (p.clusterIds) p.clusterIds[out] = cid;
-                }
-            }
-            run += chunkTotal;
+            ++q;
         }
+        run += total;
+    }
+    if constexpr (!TASKS) {
         if (threadIdx.x == 0 && tile == gridDim.x - 1u) {
             *p.drawCount = run;
             if (run > p.capacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
@@ -240,10 +368,20 @@ uint32_t cluster_tile_objects() { return kClObjects; }
 cudaError_t launch_cluster_cull(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s) {
     uint32_t tiles = (p.count + kClObjects - 1) / kClObjects;
     if (tiles == 0) tiles = 1;
-    cull_clusters_kernel<false><<<tiles, kClThreads, 0, s>>>(p, view);
+    cluster_test_kernel<false><<<tiles, kClThreads, 0, s>>>(p, view);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    cull_clusters_kernel<true><<<tiles, kClThreads, 0, s>>>(p, view);
+    cluster_emit_kernel<false><<<tiles, kClThreads, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cluster_tasks(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s) {
+    uint32_t tiles = (p.count + kClObjects - 1) / kClObjects;
+    if (tiles == 0) tiles = 1;
+    cluster_test_kernel<true><<<tiles, kClThreads, 0, s>>>(p, view);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    cluster_emit_kernel<true><<<tiles, kClThreads, 0, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -137,7 +137,18 @@ struct ClusterParams {
     uint32_t* clusterIds;
     uint32_t* drawCount;
     Scratch* scratch;
-    uint32_t* tileCount;  // scratch [tiles]: surviving clusters per tile
+    uint32_t* tileCount;  // scratch [tiles]: surviving clusters per tile ([tiles] uint2 {tasks, payloads} in task form)
+    // task form (blz_cull_cluster_tasks)
+    uint32_t* tasks;         // BlzIndirectTask words, 4 per task
+    uint32_t* payloads;      // BlzMeshTaskPayload words, 33 per payload
+    uint32_t taskCapacity;
+    uint32_t payloadCapacity;
+    uint32_t* taskCount;
+    uint32_t* payloadCount;
+    uint32_t* objSurv;       // scratch [tiles * objects per tile]: surviving clusters per object
+    uint2* objInfo;          // scratch [tiles * objects per tile]: {clusterOffset, clusterCount} of the chosen LOD
+    uint32_t* bits;          // scratch [tiles * bitWords]: one visibility bit per candidate cluster, slot order
+    uint32_t bitWords;       // words per tile: >= 32 objects x the largest LOD cluster count / 32
 };
 
 struct PyramidBuildParams {
@@ -186,6 +197,7 @@ cudaError_t launch_instanced_staged(const PipeParams& p, const InstStagedParams&
 cudaError_t launch_instanced_cull(const InstancedParams& p, const BlzCameraViewData& view, cudaStream_t s);
 uint32_t cluster_tile_objects();
 cudaError_t launch_cluster_cull(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s);
+cudaError_t launch_cluster_tasks(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s);
 cudaError_t launch_pyramid_build(const PyramidBuildParams& p, cudaStream_t s, uint32_t* launches);
 cudaError_t launch_transforms_scatter(BlzMeshTransform* table, uint32_t tableCount, const uint32_t* ids,
                                       const BlzMeshTransform* in, uint32_t n, unsigned int* status, cudaStream_t s);

@@ -64,6 +64,35 @@ class Target:
         return n, recs
 
 
+@dataclass
+class TaskTarget:
+    """Mesh-shader output of the cluster cull: IndirectTask records (ShaderBuffers.glsl:86-92), their
+    MeshTaskPayloads (ShaderBuffers.glsl:203-206) and the two counts."""
+    tasks: torch.Tensor
+    payloads: torch.Tensor
+    counts: torch.Tensor  # [taskCount, payloadCount]
+    task_capacity: int
+    payload_capacity: int
+
+    @classmethod
+    def alloc(cls, task_capacity: int, payload_capacity: int, device="cuda") -> "TaskTarget":
+        return cls(torch.zeros(max(int(task_capacity), 1) * 4, dtype=torch.int32, device=device),
+                   torch.zeros(max(int(payload_capacity), 1) * 33, dtype=torch.int32, device=device),
+                   _dev_u32(2, device), int(task_capacity), int(payload_capacity))
+
+    def ctype(self) -> abi.TaskTarget:
+        return abi.TaskTarget(self.tasks.data_ptr(), self.payloads.data_ptr(), self.task_capacity,
+                              self.payload_capacity, self.counts.data_ptr(), self.counts.data_ptr() + 4)
+
+    def read(self) -> tuple[int, int, np.ndarray, np.ndarray]:
+        """(taskCount, payloadCount, tasks[n, 4], payloads[m, 33]) as uint32, cut to the capacities."""
+        nt, np_ = (int(x) for x in self.counts.cpu().numpy().view(np.uint32)[:2])
+        mt, mp = min(nt, self.task_capacity), min(np_, self.payload_capacity)
+        tasks = self.tasks[: mt * 4].cpu().numpy().view(np.uint32).reshape(mt, 4)
+        payloads = self.payloads[: mp * 33].cpu().numpy().view(np.uint32).reshape(mp, 33)
+        return nt, np_, tasks, payloads
+
+
 class DevicePyramid:
     """A Hi-Z pyramid in device memory with its descriptor (BlzPyramid)."""
 
@@ -218,6 +247,15 @@ class Culler:
                                          C.byref(pyramid.desc) if pyramid else None, C.byref(t),
                                          cluster_ids.data_ptr() if cluster_ids is not None else None,
                                          _stream_ptr(stream)), "blz_cull_clusters")
+
+    def cluster_task_cull(self, view, target: TaskTarget, pyramid: DevicePyramid | None = None, objects=None,
+                          count=None, stream=None):
+        """The cluster cull in mesh-shader form (the reference's disabled OpaqueMeshShader path,
+        vulkanDraw.cpp:425-436, fed by culled meshlets)."""
+        t = target.ctype()
+        check(self.lib.blz_cull_cluster_tasks(self.ctx, C.byref(view), self._list(objects, count),
+                                              C.byref(pyramid.desc) if pyramid else None, C.byref(t),
+                                              _stream_ptr(stream)), "blz_cull_cluster_tasks")
 
     def raster_boxes(self, view, boxes: torch.Tensor, depth: torch.Tensor, width: int, height: int, stream=None):
         check(self.lib.blz_depth_raster_boxes(self.ctx, C.byref(view), boxes.data_ptr(), boxes.numel() // 6,

@@ -116,7 +116,11 @@ typedef struct BlzSceneDesc {
  * layouts. Replaces StaticBuffersInit / SetupForRendering
  * (src/Renderer/BlitzenVulkan/vulkanRendererSetup.cpp:453-522, dx12Renderer.h:22-43).
  * Borrowed device tables must be aligned: transforms to 32 bytes (one transform is read in a
- * single 32-byte load), surfaces, LODs and clusters to 16, render objects to 8. */
+ * single 32-byte load), surfaces, LODs and clusters to 16, render objects to 8.
+ * The LOD table is read once here (a borrowed one too, synchronously) for its largest cluster
+ * range, which sizes the cluster cull's visibility bits: a LOD whose clusterCount is raised past
+ * that afterwards makes the cluster culls skip the objects around it and raise
+ * BLZ_FLAG_BAD_INDEX. */
 int blz_scene_upload(blz_ctx* ctx, const BlzSceneDesc* scene, uint32_t flags, blz_stream_t stream);
 
 /* Device pointers of the resident tables (for callers that build render lists on the device). */
@@ -250,6 +254,32 @@ int blz_cull_instanced(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderLis
 int blz_cull_clusters(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
                       const BlzPyramid* pyramid, const BlzCullTarget* target, uint32_t* dClusterIds,
                       blz_stream_t stream);
+
+typedef struct BlzTaskTarget {
+    BlzIndirectTask* tasks;          /* device: one task per object with a surviving cluster */
+    BlzMeshTaskPayload* payloads;    /* device: ceil(survivors / 32) payloads per such object */
+    uint32_t taskCapacity;           /* tasks the buffer can hold */
+    uint32_t payloadCapacity;        /* payloads the buffer can hold */
+    uint32_t* taskCount;             /* device-accessible: set to the number of tasks (not accumulated) */
+    uint32_t* payloadCount;          /* device-accessible: set to the number of payloads */
+} BlzTaskTarget;
+
+/* Cluster cull into the mesh-shader form: the same object and cluster tests as blz_cull_clusters,
+ * with each object's surviving clusters packed 32 to a task payload instead of one draw per
+ * cluster. For every object o (ascending render-list index) with s >= 1 surviving clusters:
+ *   tasks[t]            = {taskId = p, groupCountX = ceil(s / 32), 1, 1}, t = objects before o
+ *                         with a surviving cluster;
+ *   payloads[p + g]     = {drawId = o, meshletIndices = surviving cluster indices 32g .. 32g+31 in
+ *                         ascending order, BLZ_NO_MESHLET past the last}, p = payloads of the
+ *                         objects before o.
+ * A task shader launched with groupCountX workgroups reads payloads[tasks[drawID].taskId +
+ * workGroupID.x] and emits one mesh workgroup per valid slot; the mesh shader reads the payload as
+ * MeshShader.mesh.glsl:22-25 does. Records past a capacity are not written; the counts are the
+ * full counts and an overflow sets BLZ_FLAG_COMMAND_OVERFLOW. The reference declares this format
+ * (ShaderBuffers.glsl:86-92,203-206; consumers MeshShader.task.glsl, MeshShader.mesh.glsl) but
+ * its writer is disabled (vulkanDraw.cpp:425-436). */
+int blz_cull_cluster_tasks(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
+                           const BlzPyramid* pyramid, const BlzTaskTarget* target, blz_stream_t stream);
 
 /* ---------------------------------------------------------------- batched views */
 

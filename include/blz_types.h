@@ -126,6 +126,27 @@ typedef struct BlzClusterDispatchData {
     uint32_t clusterId;
 } BlzClusterDispatchData;
 
+/* Mesh-shader draw record: the task id the task shader reads, followed by
+ * VkDrawMeshTasksIndirectCommandEXT (IndirectTask, VulkanShaderHeaders/ShaderBuffers.glsl:86-92;
+ * IndirectTaskData, src/Renderer/BlitzenVulkan/vulkanData.h:435-439). Stride 16; the indirect
+ * draw reads the group counts at offset 4. */
+typedef struct BlzIndirectTask {
+    uint32_t taskId;
+    uint32_t groupCountX;
+    uint32_t groupCountY;
+    uint32_t groupCountZ;
+} BlzIndirectTask;
+
+/* Task-to-mesh amplification payload: the draw and up to 32 meshlets, one mesh workgroup per
+ * meshlet (MeshTaskPayload, VulkanShaderHeaders/ShaderBuffers.glsl:203-206). 132 bytes. Slots
+ * past the last meshlet of a payload hold BLZ_NO_MESHLET. */
+typedef struct BlzMeshTaskPayload {
+    uint32_t drawId;
+    uint32_t meshletIndices[32];
+} BlzMeshTaskPayload;
+
+#define BLZ_NO_MESHLET 0xFFFFFFFFu
+
 /* The 256-byte cull uniform. Matrices are column-major: element (row r, column c) is
  * data[c * 4 + r], translation in data[12..14]. */
 typedef struct BlzCameraViewData {

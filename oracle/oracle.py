@@ -138,6 +138,37 @@ def cull_clusters(view, scene, pyramid: HostPyramid | None = None, stride: int =
     return int(cnt), out[:min(cnt, cap)], ids[:min(cnt, cap)], int(flags.value)
 
 
+def cluster_tasks(view, scene, pyramid: HostPyramid | None = None, objects=None, threads: int = 1):
+    """The cluster cull in mesh-shader form, restated from the cluster records: every object with s
+    surviving clusters gets one IndirectTask {first payload, ceil(s/32), 1, 1}
+    (VulkanShaderHeaders/ShaderBuffers.glsl:86-92) and ceil(s/32) MeshTaskPayloads {drawId,
+    meshletIndices[32]} (ShaderBuffers.glsl:203-206) holding its surviving cluster ids in order,
+    0xFFFFFFFF past the last. Objects in ascending render-list order. Returns (tasks[n, 4],
+    payloads[m, 33]) as uint32."""
+    cap = _cluster_upper_bound(scene, _objects_of(scene, objects))
+    n, recs, ids, _ = cull_clusters(view, scene, pyramid=pyramid, capacity=cap, objects=objects, threads=threads)
+    obj = recs[:, 0].astype(np.int64)
+    if n == 0:
+        return np.zeros((0, 4), np.uint32), np.zeros((0, 33), np.uint32)
+    starts = np.flatnonzero(np.r_[True, obj[1:] != obj[:-1]])
+    sizes = np.diff(np.r_[starts, n])
+    k = (sizes + 31) // 32
+    first = np.r_[0, np.cumsum(k)[:-1]]
+    tasks = np.stack([first, k, np.ones_like(k), np.ones_like(k)], axis=1).astype(np.uint32)
+    payloads = np.full((int(k.sum()), 33), 0xFFFFFFFF, np.uint32)
+    # survivor j of its object's run lands in payload first + j // 32, slot j % 32
+    run_of = np.repeat(np.arange(len(starts)), sizes)
+    j = np.arange(n) - starts[run_of]
+    pi = first[run_of] + j // 32
+    payloads[pi, 1 + j % 32] = ids
+    payloads[:, 0] = np.repeat(obj[starts], k)
+    return tasks, payloads
+
+
+def _objects_of(scene, objects):
+    return scene.objects if objects is None else np.ascontiguousarray(objects)
+
+
 def _cluster_upper_bound(scene, objs) -> int:
     per_surface = np.zeros(len(scene.surfaces), np.int64)
     for s in range(len(scene.surfaces)):

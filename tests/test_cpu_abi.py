@@ -48,11 +48,13 @@ int main(void) {
   S(BlzRenderObject) S(BlzMeshTransform) S(BlzPrimitiveSurface) S(BlzLodData) S(BlzLodInstanceCounter)
   S(BlzCluster) S(BlzIndirectDraw) S(BlzDrawCmd) S(BlzClusterDispatchData) S(BlzCameraViewData)
   S(BlzSceneDesc) S(BlzPyramid) S(BlzRenderList) S(BlzCullTarget) S(BlzBatchView) S(BlzLaunchShape)
-  S(BlzServeConfig) S(BlzServeRequest) S(BlzServeResult) S(BlzServeStats)
+  S(BlzServeConfig) S(BlzServeRequest) S(BlzServeResult) S(BlzServeStats) S(BlzTaskTarget)
+  S(BlzIndirectTask) S(BlzMeshTaskPayload)
   O(BlzCameraViewData, lodTarget) O(BlzCameraViewData, zNear) O(BlzCameraViewData, pyramidWidth)
   O(BlzBatchView, mode) O(BlzBatchView, visibility) O(BlzBatchView, pyramid) O(BlzBatchView, target)
   O(BlzBatchView, dynamicTransforms) O(BlzServeRequest, rotateAxes) O(BlzPyramid, mipOffset)
-  O(BlzCluster, coneAxisX) O(BlzCluster, dataOffset) O(BlzLodData, error)
+  O(BlzCluster, coneAxisX) O(BlzCluster, dataOffset) O(BlzLodData, error) O(BlzTaskTarget, taskCount)
+  O(BlzTaskTarget, payloadCapacity)
   return 0;
 }
 """
@@ -78,7 +80,8 @@ def test_struct_sizes_match_c(c_layout):
         assert C.sizeof(cls) == c_layout[name], name
     for dt, name in ((abi.RENDER_OBJECT, "BlzRenderObject"), (abi.MESH_TRANSFORM, "BlzMeshTransform"),
                      (abi.PRIMITIVE_SURFACE, "BlzPrimitiveSurface"), (abi.LOD_DATA, "BlzLodData"),
-                     (abi.LOD_INSTANCE_COUNTER, "BlzLodInstanceCounter"), (abi.CLUSTER, "BlzCluster")):
+                     (abi.LOD_INSTANCE_COUNTER, "BlzLodInstanceCounter"), (abi.CLUSTER, "BlzCluster"),
+                     (abi.INDIRECT_TASK, "BlzIndirectTask"), (abi.MESH_TASK_PAYLOAD, "BlzMeshTaskPayload")):
         assert dt.itemsize == c_layout[name], name
     assert c_layout["BlzIndirectDraw"] == abi.STRIDE_VULKAN and c_layout["BlzDrawCmd"] == abi.STRIDE_D3D12
 

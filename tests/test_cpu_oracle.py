@@ -110,3 +110,28 @@ def test_oracle_against_reference_shaders_live(seed):
         assert np.array_equal(recs, out[:m]), kind
         if vis_o is not None:
             assert np.array_equal(vis_o, vis_r), kind
+
+
+def test_cluster_task_form_groups_the_cluster_records():
+    """The oracle's mesh-shader form against a direct loop over the per-cluster records: one task
+    per object with survivors, payloads of 32 in order, 0xFFFFFFFF past the last survivor."""
+    sc = S.cluster_scene(400, seed=3, clusters_per_mesh=120)
+    v = O.view_setup(S.fov_radians(), 1920.0, 1080.0, 0.1, 1e4, position=(0.0, 0.0, -50.0))
+    tasks, payloads = O.cluster_tasks(v, sc)
+    n, recs, ids, _ = O.cull_clusters(v, sc, capacity=O._cluster_upper_bound(sc, sc.objects))
+    runs: dict[int, list[int]] = {}
+    for obj, cid in zip(recs[:, 0].tolist(), ids.tolist()):
+        runs.setdefault(obj, []).append(cid)
+    want_t, want_p = [], []
+    for obj in sorted(runs):
+        cl = runs[obj]
+        want_t.append([len(want_p), (len(cl) + 31) // 32, 1, 1])
+        for g in range(0, len(cl), 32):
+            part = cl[g:g + 32]
+            want_p.append([obj] + part + [abi.NO_MESHLET] * (32 - len(part)))
+    assert n > 0 and any(len(cl) > 32 for cl in runs.values())
+    assert np.array_equal(tasks, np.array(want_t, np.uint32).reshape(-1, 4))
+    assert np.array_equal(payloads, np.array(want_p, np.uint32).reshape(-1, 33))
+    # no survivors: empty arrays
+    t0, p0 = O.cluster_tasks(v, sc, objects=sc.objects[:0])
+    assert t0.shape == (0, 4) and p0.shape == (0, 33)

@@ -8,7 +8,7 @@ import torch
 from blitzen_gb300 import abi
 from blitzen_gb300 import scenes as S
 from blitzen_gb300.abi import BatchView, RenderList
-from blitzen_gb300.culler import Culler, DevicePyramid, Target, to_device
+from blitzen_gb300.culler import Culler, DevicePyramid, Target, TaskTarget, to_device
 from oracle import oracle as O
 from tests.helpers import H, W, assert_records_equal, view_for
 
@@ -165,6 +165,73 @@ def test_cluster_cone_test_culls_something(cluster_ctx):
     open_cones.clusters["coneCutoff"] = 127
     n_open, _, _, _ = O.cull_clusters(v, open_cones, capacity=cap)
     assert n < n_open
+
+
+def _cluster_pyramid(c, sc, v):
+    depth = O.depth_raster(v, sc.boxes, W, H)
+    pyr = DevicePyramid(W, H)
+    c.generate_depth_pyramid(pyr, torch.from_numpy(depth).cuda())
+    return pyr, O.pyramid_build(depth)
+
+
+@pytest.mark.parametrize("with_hiz", [False, True])
+def test_cluster_tasks_match_oracle(cluster_ctx, with_hiz):
+    """Mesh-shader form: IndirectTask + MeshTaskPayload records equal the oracle's, word for word
+    (unused payload slots included), and carry the same clusters as the per-cluster records."""
+    c, sc = cluster_ctx
+    v = view_for(zfar=1e4, position=(0.0, 0.0, -50.0))
+    pyr, opyr = _cluster_pyramid(c, sc, v) if with_hiz else (None, None)
+    tasks, payloads = O.cluster_tasks(v, sc, pyramid=opyr)
+    assert len(tasks) > 50 and len(payloads) > len(tasks)  # objects with more than 32 survivors occur
+    t = TaskTarget.alloc(sc.count, len(payloads) + 7)
+    t.payloads.fill_(0x5A5A5A5A)  # every word of a written payload must be overwritten
+    c.cluster_task_cull(v, t, pyramid=pyr)
+    assert c.check() == 0
+    nt, np_, gt, gp = t.read()
+    assert (nt, np_) == (len(tasks), len(payloads))
+    assert np.array_equal(gt, tasks)
+    assert np.array_equal(gp, payloads)
+    # the payloads list exactly the clusters the per-cluster records name
+    cap = O._cluster_upper_bound(sc, sc.objects)
+    n, _, oids, _ = O.cull_clusters(v, sc, pyramid=opyr, capacity=cap)
+    flat = gp[:, 1:].reshape(-1)
+    assert np.array_equal(flat[flat != abi.NO_MESHLET], oids)
+
+
+def test_cluster_tasks_subset_and_empty(cluster_ctx):
+    c, sc = cluster_ctx
+    v = view_for(zfar=1e4, position=(0.0, 0.0, -50.0))
+    objs = sc.objects[np.random.default_rng(5).permutation(sc.count)[:777]]
+    dobjs = to_device(objs, "cuda")
+    tasks, payloads = O.cluster_tasks(v, sc, objects=objs)
+    t = TaskTarget.alloc(len(objs), max(len(payloads), 1))
+    c.cluster_task_cull(v, t, objects=dobjs, count=len(objs))
+    assert c.check() == 0
+    nt, np_, gt, gp = t.read()
+    assert (nt, np_) == (len(tasks), len(payloads))
+    assert np.array_equal(gt, tasks) and np.array_equal(gp, payloads)
+    # an empty list writes zero counts
+    t.counts.fill_(-1)
+    c.cluster_task_cull(v, t, objects=dobjs, count=0)
+    assert c.check() == 0
+    assert t.read()[:2] == (0, 0)
+
+
+def test_cluster_tasks_overflow_keeps_prefix(cluster_ctx):
+    c, sc = cluster_ctx
+    v = view_for(zfar=1e4, position=(0.0, 0.0, -50.0))
+    tasks, payloads = O.cluster_tasks(v, sc)
+    nt_cap, np_cap = len(tasks) // 3, len(payloads) // 2
+    t = TaskTarget.alloc(nt_cap, np_cap)
+    c.cluster_task_cull(v, t)
+    flags = c.flags()
+    nt, np_, gt, gp = t.read()
+    assert (nt, np_) == (len(tasks), len(payloads))
+    assert np.array_equal(gt, tasks[:nt_cap])
+    # payloads that were written completely match (a payload whose object's tail lies past the
+    # capacity is still complete: each payload is written only by its own object)
+    assert np.array_equal(gp, payloads[:np_cap])
+    assert flags & abi.FLAG_COMMAND_OVERFLOW
 
 
 # ----------------------------------------------------------------------------- batch
