@@ -110,17 +110,23 @@ int ensure_chunk_scratch(blz_ctx* c, size_t chunks, size_t chunkSize) {
     return BLZ_OK;
 }
 
-// Cluster-cull scratch for `tiles` tiles: tile counts (uint2), object ranges (uint2) and survivor
-// counts per object, then the visibility bits (bitWords per tile). Grown on demand like the
+// Cluster-cull scratch for `tiles` tiles: counts and their exclusive prefix per tile (uint2),
+// candidates per tile, the
+// objects' cluster ranges, transforms and survivor counts, then the visibility bits (bitWords per
+// tile). Grown on demand like the
 // object-cull scratch.
 int bind_cluster_scratch(blz_ctx* c, uint32_t tiles, ClusterParams& p) {
     const size_t objs = static_cast<size_t>(tiles) * cluster_tile_objects();
     const uint32_t bitWords = std::max<uint32_t>(c->lodClusterMax, 1u);  // 32 objects x max clusters / 32 bits
-    const size_t countBytes = (static_cast<size_t>(tiles) * sizeof(uint2) + 255) & ~size_t(255);
-    const size_t infoBytes = (objs * sizeof(uint2) + 255) & ~size_t(255);
-    const size_t survBytes = (objs * sizeof(uint32_t) + 255) & ~size_t(255);
+    const uint32_t split = cluster_split(c->lodClusterMax);
+    auto r256 = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t countBytes = r256(static_cast<size_t>(tiles) * sizeof(uint2));
+    const size_t tileBytes = r256(static_cast<size_t>(tiles) * sizeof(uint32_t));
+    const size_t infoBytes = r256(objs * sizeof(uint2));
+    const size_t xfBytes = r256(objs * 2 * sizeof(float4));
+    const size_t survBytes = r256(objs * sizeof(uint32_t));
     const size_t bitBytes = static_cast<size_t>(tiles) * bitWords * sizeof(uint32_t);
-    const size_t need = countBytes + infoBytes + survBytes + bitBytes;
+    const size_t need = 2 * countBytes + tileBytes + infoBytes + xfBytes + survBytes + bitBytes;
     if (need > c->clusterBytes) {
         if (c->capturing) return fail(BLZ_ERR_CAPACITY, "scratch must grow, which a capture cannot record: run the call once before capturing");
         if (c->clusterMem) {
@@ -136,10 +142,21 @@ int bind_cluster_scratch(blz_ctx* c, uint32_t tiles, ClusterParams& p) {
     }
     char* m = static_cast<char*>(c->clusterMem);
     p.tileCount = reinterpret_cast<uint32_t*>(m);
-    p.objInfo = reinterpret_cast<uint2*>(m + countBytes);
-    p.objSurv = reinterpret_cast<uint32_t*>(m + countBytes + infoBytes);
-    p.bits = reinterpret_cast<uint32_t*>(m + countBytes + infoBytes + survBytes);
+    m += countBytes;
+    p.tilePrefix = reinterpret_cast<uint2*>(m);
+    m += countBytes;
+    p.tileSlots = reinterpret_cast<uint32_t*>(m);
+    m += tileBytes;
+    p.objInfo = reinterpret_cast<uint2*>(m);
+    m += infoBytes;
+    p.objXf = reinterpret_cast<float4*>(m);
+    m += xfBytes;
+    p.objSurv = reinterpret_cast<uint32_t*>(m);
+    m += survBytes;
+    p.bits = reinterpret_cast<uint32_t*>(m);
     p.bitWords = bitWords;
+    p.tiles = tiles;
+    p.split = split;
     return BLZ_OK;
 }
 
@@ -652,7 +669,7 @@ int blz_cull_clusters(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList l
     p.scratch = c->scratch;
     cudaError_t e = launch_cluster_cull(p, *view, reinterpret_cast<cudaStream_t>(s));
     if (e != cudaSuccess) return cuda_fail(e, "cluster cull launch");
-    c->launches += 2;  // count, write
+    c->launches += 4;  // objects, tests, scan, emit
     return BLZ_OK;
 }
 
@@ -692,7 +709,7 @@ int blz_cull_cluster_tasks(blz_ctx* c, const BlzCameraViewData* view, BlzRenderL
     p.payloadCount = target->payloadCount;
     cudaError_t e = launch_cluster_tasks(p, *view, reinterpret_cast<cudaStream_t>(s));
     if (e != cudaSuccess) return cuda_fail(e, "cluster task cull launch");
-    c->launches += 2;  // count, write
+    c->launches += 5;  // objects, tests, task totals, scan, emit
     return BLZ_OK;
 }
 

@@ -137,7 +137,7 @@ struct ClusterParams {
     uint32_t* clusterIds;
     uint32_t* drawCount;
     Scratch* scratch;
-    uint32_t* tileCount;  // scratch [tiles]: surviving clusters per tile ([tiles] uint2 {tasks, payloads} in task form)
+    uint32_t* tileCount;  // scratch [tiles] uint2: {surviving clusters, 0} per tile (task form: {tasks, payloads})
     // task form (blz_cull_cluster_tasks)
     uint32_t* tasks;         // BlzIndirectTask words, 4 per task
     uint32_t* payloads;      // BlzMeshTaskPayload words, 33 per payload
@@ -147,8 +147,13 @@ struct ClusterParams {
     uint32_t* payloadCount;
     uint32_t* objSurv;       // scratch [tiles * objects per tile]: surviving clusters per object
     uint2* objInfo;          // scratch [tiles * objects per tile]: {clusterOffset, clusterCount} of the chosen LOD
+    float4* objXf;           // scratch [tiles * objects per tile * 2]: the object's transform {pos, scale}, {quat}
     uint32_t* bits;          // scratch [tiles * bitWords]: one visibility bit per candidate cluster, slot order
     uint32_t bitWords;       // words per tile: >= 32 objects x the largest LOD cluster count / 32
+    uint32_t tiles;          // tiles of 32 objects
+    uint32_t split;          // test blocks per tile
+    uint32_t* tileSlots;     // scratch [tiles]: candidate clusters of the tile
+    uint2* tilePrefix;       // scratch [tiles]: records (task form: {tasks, payloads}) before the tile
 };
 
 struct PyramidBuildParams {
@@ -196,6 +201,7 @@ cudaError_t launch_instanced_staged(const PipeParams& p, const InstStagedParams&
                                     int smCount, cudaStream_t s);
 cudaError_t launch_instanced_cull(const InstancedParams& p, const BlzCameraViewData& view, cudaStream_t s);
 uint32_t cluster_tile_objects();
+uint32_t cluster_split(uint32_t lodClusterMax);
 cudaError_t launch_cluster_cull(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s);
 cudaError_t launch_cluster_tasks(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s);
 cudaError_t launch_pyramid_build(const PyramidBuildParams& p, cudaStream_t s, uint32_t* launches);
