@@ -309,151 +309,127 @@ __global__ void __launch_bounds__(kClThreads) cluster_task_totals_kernel(const C
     if (lane == 0) reinterpret_cast<uint2*>(p.tileCount)[tile] = make_uint2(tasks, payloads);
 }
 
-// Emit launch, one block per tile: no test is repeated. The tile's cluster ranges, visibility bits
-// and the records (task form: tasks and payloads) before it come from the earlier launches; every
-// set bit is written at its final position in slot order, the warp's set bits spread over its
-// lanes.
+// Emit launch, one warp per tile (lane = object): no test is repeated. The tile's cluster ranges,
+// visibility bits and the records (task form: tasks and payloads) before it come from the earlier
+// launches; every set bit is written at its final position in slot order, the tile's set bits
+// spread over the lanes 32 at a time.
 template <bool TASKS>
 __global__ void __launch_bounds__(kClThreads) cluster_emit_kernel(const ClusterParams p) {
-    __shared__ uint32_t s_start[kClObjects + 1];
-    __shared__ uint32_t s_off[kClObjects];
-    __shared__ uint32_t s_first[kClObjects];  // task form: the object's first payload
-    __shared__ uint32_t s_rank[kClObjects];   // task form: survivors of the tile before the object
-    __shared__ uint32_t s_warp[kClWarps];
-    __shared__ uint32_t s_base;
-    const uint32_t tile = blockIdx.x;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t tile = blockIdx.x * kClWarps + warp;
+    if (tile >= p.tiles) return;
     const uint32_t lt = lanemask_lt();
     const uint32_t* bits = p.bits + static_cast<size_t>(tile) * p.bitWords;
 
-    // independent loads first: the tile's candidates, its first round of bit words, the object
-    // ranges and the records before the tile (warp 0)
+    // independent loads first
     const uint32_t T = __ldcg(p.tileSlots + tile);
-    const uint32_t bFirst = threadIdx.x < p.bitWords ? __ldcg(bits + threadIdx.x) : 0u;
-    uint2 info = make_uint2(0u, 0u), pre = make_uint2(0u, 0u);
-    uint32_t sv = 0;
-    if (warp == 0) {
-        info = __ldcg(p.objInfo + tile * kClObjects + lane);  // {clusterOffset, count}
-        pre = __ldcg(p.tilePrefix + tile);                    // records (tasks, payloads) before the tile
-        if constexpr (TASKS) sv = __ldcg(p.objSurv + tile * kClObjects + lane);
-        const uint32_t base = pre.x, baseP = pre.y;
-        uint32_t incl = info.y;
+    const uint32_t bFirst = lane < p.bitWords ? __ldcg(bits + lane) : 0u;
+    const uint2 info = __ldcg(p.objInfo + tile * kClObjects + lane);  // {clusterOffset, count}
+    const uint2 pre = __ldcg(p.tilePrefix + tile);                    // records (tasks, payloads) before the tile
+    const uint32_t sv = TASKS ? __ldcg(p.objSurv + tile * kClObjects + lane) : 0u;
+
+    uint32_t incl = info.y;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= static_cast<uint32_t>(d)) incl += n;
+    }
+    const uint32_t start = incl - info.y;  // the object's first slot
+    uint32_t first = 0, before = 0;        // task form: first payload, the tile's survivors before the object
+    if constexpr (TASKS) {
+        const uint32_t k = (sv + 31u) >> 5;
+        uint32_t is = sv, ik = k;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-            if (lane >= static_cast<uint32_t>(d)) incl += n;
+            const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, is, d);
+            const uint32_t b = __shfl_up_sync(0xFFFFFFFFu, ik, d);
+            if (lane >= static_cast<uint32_t>(d)) {
+                is += a;
+                ik += b;
+            }
         }
-        s_start[lane] = incl - info.y;
-        s_off[lane] = info.x;
-        if (lane == 31) s_start[kClObjects] = incl;
-        if constexpr (TASKS) {
-            // per object: its task slot, first payload and the tile's survivors before it
-            const uint32_t k = (sv + 31u) >> 5;
-            uint32_t is = sv, ik = k;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, is, d);
-                const uint32_t b = __shfl_up_sync(0xFFFFFFFFu, ik, d);
-                if (lane >= static_cast<uint32_t>(d)) {
-                    is += a;
-                    ik += b;
-                }
+        const unsigned has = __ballot_sync(0xFFFFFFFFu, sv != 0u);
+        first = pre.y + ik - k;
+        before = is - sv;
+        if (sv != 0u) {
+            const uint32_t t = pre.x + __popc(has & lt);
+            if (t < p.taskCapacity) {
+                uint32_t* tw = p.tasks + static_cast<size_t>(t) * 4u;
+                tw[0] = first;
+                tw[1] = k;
+                tw[2] = 1u;
+                tw[3] = 1u;
             }
-            const unsigned has = __ballot_sync(0xFFFFFFFFu, sv != 0u);
-            const uint32_t first = baseP + ik - k;
-            s_rank[lane] = is - sv;
-            s_first[lane] = first;
-            if (sv != 0u) {
-                const uint32_t t = base + __popc(has & lt);
-                if (t < p.taskCapacity) {
-                    uint32_t* tw = p.tasks + static_cast<size_t>(t) * 4u;
-                    tw[0] = first;
-                    tw[1] = k;
-                    tw[2] = 1u;
-                    tw[3] = 1u;
-                }
-                const uint32_t tail = sv & 31u;  // the last payload's unused slots
-                const uint32_t last = first + k - 1u;
-                if (tail != 0u && last < p.payloadCapacity) {
-                    uint32_t* pw = p.payloads + static_cast<size_t>(last) * 33u + 1u;
-                    for (uint32_t e = tail; e < 32u; ++e) pw[e] = BLZ_NO_MESHLET;
-                }
+            const uint32_t tail = sv & 31u;  // the last payload's unused slots
+            const uint32_t last = first + k - 1u;
+            if (tail != 0u && last < p.payloadCapacity) {
+                uint32_t* pw = p.payloads + static_cast<size_t>(last) * 33u + 1u;
+                for (uint32_t e = tail; e < 32u; ++e) pw[e] = BLZ_NO_MESHLET;
             }
-            if (lane == 31 && tile == gridDim.x - 1u) {
-                const uint32_t nt = base + __popc(has), np = baseP + ik;
-                *p.taskCount = nt;
-                *p.payloadCount = np;
-                if (nt > p.taskCapacity || np > p.payloadCapacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
-            }
-        } else if (lane == 0) {
-            s_base = base;
+        }
+        if (lane == 31 && tile == p.tiles - 1u) {
+            const uint32_t nt = pre.x + __popc(has), np = pre.y + ik;
+            *p.taskCount = nt;
+            *p.payloadCount = np;
+            if (nt > p.taskCapacity || np > p.payloadCapacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
         }
     }
-    __syncthreads();
+
     const uint32_t words = (T + 31u) >> 5;
-    uint32_t run = TASKS ? 0u : s_base;  // records before the current round of words
-    for (uint32_t w0 = 0; w0 < words; w0 += kClThreads) {
-        const uint32_t w = w0 + threadIdx.x;
-        const uint32_t b = w >= words ? 0u : (w0 == 0 ? bFirst : __ldcg(bits + w));
+    uint32_t run = TASKS ? 0u : pre.x;  // records (task form: the tile's survivors) before this round
+    uint32_t bNext = lane < words ? bFirst : 0u;
+    for (uint32_t w0 = 0; w0 < words; w0 += 32u) {
+        const uint32_t b = bNext;  // this round's word; the next round's is loaded ahead
+        bNext = w0 + 32u + lane < words ? __ldcg(bits + w0 + 32u + lane) : 0u;
         const uint32_t c = __popc(b);
-        uint32_t incl = c;
+        uint32_t wincl = c;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-            if (lane >= static_cast<uint32_t>(d)) incl += n;
+            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, wincl, d);
+            if (lane >= static_cast<uint32_t>(d)) wincl += n;
         }
-        const uint32_t excl = incl - c;
-        if (w0 != 0) __syncthreads();  // the previous round's s_warp reads are done
-        if (lane == 31) s_warp[warp] = incl;
-        __syncthreads();
-        uint32_t wbase = run, total = 0;
-#pragma unroll
-        for (int ww = 0; ww < kClWarps; ++ww) {
-            const uint32_t n = s_warp[ww];
-            if (ww < static_cast<int>(warp)) wbase += n;
-            total += n;
-        }
-        // the warp's set bits spread over its lanes: lane L takes set bit k0 + L of the warp's words
-        const uint32_t warpTotal = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        for (uint32_t k0 = 0; k0 < warpTotal; k0 += 32u) {
-            const uint32_t k = k0 + lane;
-            uint32_t j = 0;  // the warp's word holding set bit k: the number of words with incl <= k
+        const uint32_t wexcl = wincl - c;
+        const uint32_t roundTotal = __shfl_sync(0xFFFFFFFFu, wincl, 31);
+        for (uint32_t k0 = 0; k0 < roundTotal; k0 += 32u) {
+            const uint32_t k = k0 + lane;  // the round's set bit taken by this lane
+            uint32_t j = 0;                // its word: the number of words with wincl <= k
 #pragma unroll
             for (uint32_t step = 16; step > 0; step >>= 1)
-                if (__shfl_sync(0xFFFFFFFFu, incl, j + step - 1u) <= k) j += step;
+                if (__shfl_sync(0xFFFFFFFFu, wincl, j + step - 1u) <= k) j += step;
             const uint32_t wj = __shfl_sync(0xFFFFFFFFu, b, j);
-            const uint32_t ej = __shfl_sync(0xFFFFFFFFu, excl, j);
-            if (k < warpTotal) {
-                const uint32_t slot = (w0 + warp * 32u + j) * 32u + nth_set_bit(wj, k - ej);
-                const uint32_t lo = slot_object(s_start, slot);
-                const uint32_t cid = s_off[lo] + (slot - s_start[lo]);
-                const uint32_t q = wbase + k;
-                if constexpr (TASKS) {
-                    const uint32_t rank = q - s_rank[lo];
-                    const uint32_t pi = s_first[lo] + (rank >> 5);
-                    if (pi < p.payloadCapacity) {
-                        uint32_t* pw = p.payloads + static_cast<size_t>(pi) * 33u;
-                        pw[1u + (rank & 31u)] = cid;
-                        if ((rank & 31u) == 0u) pw[0] = tile * kClObjects + lo;
-                    }
-                } else if (q < p.capacity) {
-                    // InitialClusterCull.comp.glsl:48-54: {objectId, triangleCount * 3, 1, dataOffset, 0, 0}
-                    const uint4 meta = __ldg(reinterpret_cast<const uint4*>(p.sc.clusters + cid) + 1);
-                    uint32_t* rec = reinterpret_cast<uint32_t*>(p.cmds + static_cast<size_t>(q) * p.stride);
-                    rec[0] = tile * kClObjects + lo;
-                    rec[1] = ((meta.z >> 8) & 0xFFu) * 3u;
-                    rec[2] = 1u;
-                    rec[3] = meta.y;
-                    rec[4] = 0u;
-                    rec[5] = 0u;
-                    if (p.clusterIds) p.clusterIds[q] = cid;
+            const uint32_t ej = __shfl_sync(0xFFFFFFFFu, wexcl, j);
+            const uint32_t slot = (w0 + j) * 32u + (k < roundTotal ? nth_set_bit(wj, k - ej) : 0u);
+            uint32_t lo = 0;  // its object: the last one whose first slot is <= slot
+#pragma unroll
+            for (uint32_t step = 16; step > 0; step >>= 1)
+                if (__shfl_sync(0xFFFFFFFFu, start, lo + step) <= slot) lo += step;
+            const uint32_t cid = __shfl_sync(0xFFFFFFFFu, info.x, lo) + (slot - __shfl_sync(0xFFFFFFFFu, start, lo));
+            const uint32_t q = run + k;
+            if constexpr (TASKS) {
+                const uint32_t rank = q - __shfl_sync(0xFFFFFFFFu, before, lo);
+                const uint32_t pi = __shfl_sync(0xFFFFFFFFu, first, lo) + (rank >> 5);
+                if (k < roundTotal && pi < p.payloadCapacity) {
+                    uint32_t* pw = p.payloads + static_cast<size_t>(pi) * 33u;
+                    pw[1u + (rank & 31u)] = cid;
+                    if ((rank & 31u) == 0u) pw[0] = tile * kClObjects + lo;
                 }
+            } else if (k < roundTotal && q < p.capacity) {
+                // InitialClusterCull.comp.glsl:48-54: {objectId, triangleCount * 3, 1, dataOffset, 0, 0}
+                const uint4 meta = __ldg(reinterpret_cast<const uint4*>(p.sc.clusters + cid) + 1);
+                uint32_t* rec = reinterpret_cast<uint32_t*>(p.cmds + static_cast<size_t>(q) * p.stride);
+                rec[0] = tile * kClObjects + lo;
+                rec[1] = ((meta.z >> 8) & 0xFFu) * 3u;
+                rec[2] = 1u;
+                rec[3] = meta.y;
+                rec[4] = 0u;
+                rec[5] = 0u;
+                if (p.clusterIds) p.clusterIds[q] = cid;
             }
         }
-        run += total;
+        run += roundTotal;
     }
     if constexpr (!TASKS) {
-        if (threadIdx.x == 0 && tile == gridDim.x - 1u) {
+        if (lane == 0 && tile == p.tiles - 1u) {
             *p.drawCount = run;
             if (run > p.capacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
         }
@@ -478,7 +454,7 @@ static cudaError_t launch_cluster(const ClusterParams& p, const BlzCameraViewDat
     cluster_scan_kernel<<<1, kScanThreads, 0, s>>>(p);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    cluster_emit_kernel<TASKS><<<p.tiles, kClThreads, 0, s>>>(p);
+    cluster_emit_kernel<TASKS><<<(p.tiles + kClWarps - 1) / kClWarps, kClThreads, 0, s>>>(p);
     return cudaGetLastError();
 }
 
