@@ -170,6 +170,7 @@ _PROTOS = {
     "blz_transforms_update": (_I, [_P, _P, _P, _U32, _P]),
     "blz_transforms_update_device": (_I, [_P, _P, _P, _U32, _P]),
     "blz_transforms_rotate": (_I, [_P, _P, _P, C.c_float, _U32, _P, _P]),
+    "blz_scene_bind_dynamic": (_I, [_P, _P, _U32]),
     "blz_pyramid_layout": (C.c_uint64, [_U32, _U32, _U32, C.POINTER(Pyramid)]),
     "blz_pyramid_build": (_I, [_P, C.POINTER(Pyramid), _P, _P]),
     "blz_depth_raster_boxes": (_I, [_P, C.POINTER(CameraViewData), _P, _U32, _P, _U32, _U32, _P]),

@@ -330,6 +330,18 @@ int blz_scene_upload(blz_ctx* c, const BlzSceneDesc* s, uint32_t flags, blz_stre
     return BLZ_OK;
 }
 
+int blz_scene_bind_dynamic(blz_ctx* c, const BlzMeshTransform* rows, uint32_t count) {
+    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (!c->hasScene) return fail(BLZ_ERR_NO_SCENE, "no scene uploaded");
+    if (count > c->scene.transformCount)
+        return fail(BLZ_ERR_INVALID_ARGUMENT, "%u dynamic rows but the scene has %u transforms", count, c->scene.transformCount);
+    if (count > 0 && !rows) return fail(BLZ_ERR_INVALID_ARGUMENT, "rows is NULL");
+    if (reinterpret_cast<uintptr_t>(rows) % 32 != 0) return fail(BLZ_ERR_INVALID_ARGUMENT, "rows must be 32-byte aligned");
+    c->scene.dynRows = count > 0 ? rows : nullptr;
+    c->scene.dynCount = count;
+    return BLZ_OK;
+}
+
 int blz_scene_device_tables(const blz_ctx* c, BlzSceneDesc* out) {
     if (!c || !out) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or out is NULL");
     if (!c->hasScene) return fail(BLZ_ERR_NO_SCENE, "no scene uploaded");
@@ -390,7 +402,7 @@ int blz_transforms_rotate(blz_ctx* c, const uint32_t* ids, const float* axes, fl
         // in place: rotate into staging, then scatter back (a kernel may not read and write the same rows)
         return fail(BLZ_ERR_INVALID_ARGUMENT, "in-place rotation needs a destination buffer; pass dDst and scatter it");
     }
-    cudaError_t e = launch_transforms_rotate(c->scene.transforms, c->scene.transformCount, ids, axes, angle, n, out, &c->scratch->status,
+    cudaError_t e = launch_transforms_rotate(c->scene.transforms, c->scene.transformCount, c->scene.dynRows, c->scene.dynCount, ids, axes, angle, n, out, &c->scratch->status,
                                              reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "transforms rotate launch");
     if (n) c->launches++;

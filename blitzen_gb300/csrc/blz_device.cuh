@@ -275,6 +275,8 @@ struct SceneTables {
     const BlzLodData* lods;
     const BlzCluster* clusters;
     uint32_t transformCount, surfaceCount, lodCount, clusterCount;
+    const BlzMeshTransform* dynRows;  // bound dynamic rows: transforms [0, dynCount) are read here
+    uint32_t dynCount, pad0;
 };
 
 // Scratch of the single-pass kernels (one per context, zeroed once at creation).
@@ -317,6 +319,14 @@ __device__ __forceinline__ void ldg_transform(const BlzMeshTransform* t, float4&
         : "=f"(posScale.x), "=f"(posScale.y), "=f"(posScale.z), "=f"(posScale.w), "=f"(q.x), "=f"(q.y), "=f"(q.z),
           "=f"(q.w)
         : "l"(t));
+}
+
+// Transform `tid` of the scene, from the bound dynamic rows when tid < dynCount (device or pinned
+// host memory), else from the resident table: a pointer select, then one 32-byte load (both are
+// 32-byte aligned).
+__device__ __forceinline__ void load_transform(const SceneTables& sc, uint32_t tid, float4& posScale, float4& q) {
+    const BlzMeshTransform* base = tid < sc.dynCount ? sc.dynRows : sc.transforms;
+    ldg_transform(base + tid, posScale, q);
 }
 
 // Programmatic dependent launch. A kernel launched with programmatic stream serialization may be

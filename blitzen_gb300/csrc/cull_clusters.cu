@@ -103,9 +103,7 @@ __global__ void __launch_bounds__(kClThreads) cluster_object_kernel(const Cluste
         uint4 sm = make_uint4(0u, 0u, 0u, 0u);
         float4 sph = make_float4(0.f, 0.f, 0.f, 0.f);
         if (ok) {
-            const float4* tp = reinterpret_cast<const float4*>(p.sc.transforms + ro.x);
-            posScale = __ldg(tp);
-            quat = __ldg(tp + 1);
+            load_transform(p.sc, ro.x, posScale, quat);
             const float4* sp = reinterpret_cast<const float4*>(p.sc.surfaces + ro.y);
             sph = __ldg(sp);
             sm = __ldg(reinterpret_cast<const uint4*>(sp + 1));

@@ -28,8 +28,8 @@ __device__ __forceinline__ uint32_t inst_bucket(const SceneTables& sc, const Blz
         flags |= BLZ_FLAG_BAD_INDEX;
         return kNoBucket;
     }
-    const float4* tp = reinterpret_cast<const float4*>(sc.transforms + ro.x);
-    const float4 ps = __ldg(tp), q = __ldg(tp + 1);
+    float4 ps, q;
+    load_transform(sc, ro.x, ps, q);
     const float4* sp = reinterpret_cast<const float4*>(sc.surfaces + ro.y);
     const float4 sph = __ldg(sp);
     const uint4 sm = __ldg(reinterpret_cast<const uint4*>(sp + 1));

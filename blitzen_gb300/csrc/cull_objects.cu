@@ -155,11 +155,15 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
         for (int k = 0; k < OPT; ++k) {
             ok[k] = active(obj[k], vis[k]) && ro[k].x < sc.transformCount && ro[k].y < sc.surfaceCount;
             const uint32_t tid = ok[k] ? ro[k].x : 0u, sid = ok[k] ? ro[k].y : 0u;
-            const BlzMeshTransform* tt = sc.transforms;
             if constexpr (!SINGLE) {
-                if (bv.dynT != nullptr && tid < bv.dynCount) tt = bv.dynT;
+                if (bv.dynT != nullptr && tid < bv.dynCount) {  // the view's own rows first
+                    ldg_transform(bv.dynT + tid, ps[k], q[k]);
+                } else {
+                    load_transform(sc, tid, ps[k], q[k]);
+                }
+            } else {
+                load_transform(sc, tid, ps[k], q[k]);
             }
-            ldg_transform(tt + tid, ps[k], q[k]);
             if (surf.sphere != nullptr) {
                 sph[k] = surf.sphere[sid];
                 lod[k] = surf.lod[sid];

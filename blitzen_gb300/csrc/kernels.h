@@ -23,6 +23,8 @@ struct SceneTablesHost {
     const BlzLodData* lods;
     const BlzCluster* clusters;
     uint32_t transformCount, surfaceCount, lodCount, clusterCount;
+    const BlzMeshTransform* dynRows;  // bound dynamic rows: transforms [0, dynCount) are read here
+    uint32_t dynCount, pad0;
 };
 
 struct PyramidViewHost {
@@ -207,9 +209,9 @@ cudaError_t launch_cluster_tasks(const ClusterParams& p, const BlzCameraViewData
 cudaError_t launch_pyramid_build(const PyramidBuildParams& p, cudaStream_t s, uint32_t* launches);
 cudaError_t launch_transforms_scatter(BlzMeshTransform* table, uint32_t tableCount, const uint32_t* ids,
                                       const BlzMeshTransform* in, uint32_t n, unsigned int* status, cudaStream_t s);
-cudaError_t launch_transforms_rotate(const BlzMeshTransform* table, uint32_t tableCount, const uint32_t* ids,
-                                     const float* axes, float angle, uint32_t n, BlzMeshTransform* dst,
-                                     unsigned int* status, cudaStream_t s);
+cudaError_t launch_transforms_rotate(const BlzMeshTransform* table, uint32_t tableCount, const BlzMeshTransform* dynRows,
+                                     uint32_t dynCount, const uint32_t* ids, const float* axes, float angle, uint32_t n,
+                                     BlzMeshTransform* dst, unsigned int* status, cudaStream_t s);
 cudaError_t launch_depth_raster(const BlzCameraViewData& view, const float* boxes, uint32_t boxCount, float* depth,
                                 uint32_t width, uint32_t height, cudaStream_t s, uint32_t* launches);
 

@@ -26,9 +26,9 @@ __global__ void transforms_scatter_kernel(BlzMeshTransform* table, uint32_t tabl
 // dst[i] = table[ids[i]] with orientation r (x) q, r = (s * axis_i, c); the rotation of
 // src/Game/blitzenObject.cpp:30-46 applied incrementally on the device. s, c = sin/cos(angle/2)
 // are computed once on the host.
-__global__ void transforms_rotate_kernel(const BlzMeshTransform* table, uint32_t tableCount, const uint32_t* ids,
-                                         const float* axes, float s, float c, uint32_t n, BlzMeshTransform* dst,
-                                         unsigned int* status) {
+__global__ void transforms_rotate_kernel(const BlzMeshTransform* table, uint32_t tableCount, const BlzMeshTransform* dynRows,
+                                         uint32_t dynCount, const uint32_t* ids, const float* axes, float s, float c,
+                                         uint32_t n, BlzMeshTransform* dst, unsigned int* status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = ids[i];
@@ -36,7 +36,7 @@ __global__ void transforms_rotate_kernel(const BlzMeshTransform* table, uint32_t
         atomicOr(status, BLZ_FLAG_BAD_INDEX);
         return;
     }
-    const float4* src = reinterpret_cast<const float4*>(table + id);
+    const float4* src = reinterpret_cast<const float4*>((id < dynCount ? dynRows : table) + id);
     const float4 ps = src[0], q = src[1];
     const float rx = BLZ_FM(s, axes[3 * i + 0]), ry = BLZ_FM(s, axes[3 * i + 1]), rz = BLZ_FM(s, axes[3 * i + 2]);
     const float rw = c;
@@ -57,13 +57,14 @@ cudaError_t launch_transforms_scatter(BlzMeshTransform* table, uint32_t tableCou
     return cudaGetLastError();
 }
 
-cudaError_t launch_transforms_rotate(const BlzMeshTransform* table, uint32_t tableCount, const uint32_t* ids,
-                                     const float* axes, float angle, uint32_t n, BlzMeshTransform* dst,
-                                     unsigned int* status, cudaStream_t s) {
+cudaError_t launch_transforms_rotate(const BlzMeshTransform* table, uint32_t tableCount, const BlzMeshTransform* dynRows,
+                                     uint32_t dynCount, const uint32_t* ids, const float* axes, float angle, uint32_t n,
+                                     BlzMeshTransform* dst, unsigned int* status, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     const float h = angle * 0.5f;
     const float sn = sinf(h), cs = cosf(h);  // host libm, the same values the host oracle uses
-    transforms_rotate_kernel<<<(n + 255) / 256, 256, 0, s>>>(table, tableCount, ids, axes, sn, cs, n, dst, status);
+    transforms_rotate_kernel<<<(n + 255) / 256, 256, 0, s>>>(table, tableCount, dynRows, dynCount, ids, axes, sn, cs, n,
+                                                               dst, status);
     return cudaGetLastError();
 }
 

@@ -193,6 +193,16 @@ class Culler:
         check(self.lib.blz_transforms_update_device(self.ctx, ids.data_ptr(), transforms.data_ptr(),
                                                     ids.numel(), _stream_ptr(stream)), "blz_transforms_update_device")
 
+    def bind_dynamic_transforms(self, rows: torch.Tensor | None) -> None:
+        """Transforms [0, n) read from `rows` (n MeshTransform rows in device or pinned host memory)
+        by every later cull; None unbinds. The reference's dynamic objects are transforms [0, 1000)
+        rewritten each frame through a mapped staging buffer (blitRender.h:10, vulkanDraw.cpp:46-60)."""
+        if rows is None:
+            check(self.lib.blz_scene_bind_dynamic(self.ctx, None, 0), "blz_scene_bind_dynamic")
+        else:
+            check(self.lib.blz_scene_bind_dynamic(self.ctx, rows.data_ptr(), rows.numel() * rows.element_size() // 32),
+                  "blz_scene_bind_dynamic")
+
     def rotate_transforms(self, ids: torch.Tensor, axes: torch.Tensor, angle: float, dst: torch.Tensor, stream=None):
         check(self.lib.blz_transforms_rotate(self.ctx, ids.data_ptr(), axes.data_ptr(), angle, ids.numel(),
                                              dst.data_ptr(), _stream_ptr(stream)), "blz_transforms_rotate")

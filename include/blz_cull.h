@@ -146,6 +146,18 @@ int blz_transforms_update_device(blz_ctx* ctx, const uint32_t* dIds, const BlzMe
 int blz_transforms_rotate(blz_ctx* ctx, const uint32_t* dIds, const float* dAxes, float angle,
                           uint32_t n, BlzMeshTransform* dDst, blz_stream_t stream);
 
+/* Binds the scene's dynamic rows: from the next call on, every cull and blz_transforms_rotate of
+ * this context reads transforms [0, count) from rows[] instead of the resident table (count 0
+ * unbinds). rows is device-accessible memory, 32-byte aligned: device memory, or pinned host memory
+ * that the kernels read over the CPU-GPU link, so the renderer's mapped staging buffer can serve
+ * directly. The reference keeps its dynamic objects in transforms [0, 1000)
+ * (src/Renderer/blitRender.h:10), rewrites them through that staging buffer
+ * (UpdateObjectTransform, src/Renderer/BlitzenVulkan/vulkanDraw.cpp:46-60) and copies it to the
+ * device table every frame (UpdateBuffers, vulkanDraw.cpp:816-820); bound rows replace that copy.
+ * blz_transforms_update writes the resident table, which bound rows hide for ids < count. A recorded
+ * frame keeps the binding it was recorded with; blz_scene_upload unbinds. Host-side only. */
+int blz_scene_bind_dynamic(blz_ctx* ctx, const BlzMeshTransform* rows, uint32_t count);
+
 /* ---------------------------------------------------------------- depth pyramid */
 
 typedef struct BlzPyramid {

@@ -438,3 +438,109 @@ def test_serving_admission_waits_for_memory(stress_ctx):
         assert stats.peakOutputBytes <= 8 << 20
     finally:
         lib.blz_serve_destroy(server)
+
+
+# ----------------------------------------------------------------------------- bound dynamic rows
+
+def _moved_rows(sc, n, seed):
+    rng = np.random.default_rng(seed)
+    rows = sc.transforms[:n].copy()
+    rows["pos"] += rng.uniform(-400.0, 400.0, size=(n, 3)).astype(np.float32)
+    rows["orientation"] = S.random_unit_quaternions(rng, n)
+    return rows
+
+
+@pytest.mark.parametrize("where", ["pinned", "device"])
+def test_bound_dynamic_rows_match_edited_scene(stress_ctx, where):
+    """Transforms [0, n) read from bound rows (pinned host or device memory) give the oracle's
+    results on a scene whose table holds those rows; unbinding restores the resident table."""
+    c, sc = stress_ctx
+    n = 1000
+    rows = _moved_rows(sc, n, 21)
+    host = torch.from_numpy(rows.view(np.float32).reshape(-1).copy())
+    bound = host.pin_memory() if where == "pinned" else host.cuda()
+    edited = S.Scene(sc.objects, sc.transforms.copy(), sc.surfaces, sc.lods)
+    edited.transforms[:n] = rows
+    v = view_for(zfar=1e4)
+    depth = O.depth_raster(v, sc.boxes, W, H)
+    pyr = DevicePyramid(W, H)
+    c.generate_depth_pyramid(pyr, torch.from_numpy(depth).cuda())
+    opyr = O.pyramid_build(depth)
+    c.bind_dynamic_transforms(bound)
+    try:
+        t = Target.alloc(sc.count)
+        c.draw_cull(v, t)
+        assert c.check() == 0
+        assert_records_equal(t.read(), O.cull(0, v, edited)[:2], "frustum, bound rows")
+        vis0 = sc.visibility.copy()
+        dvis = torch.from_numpy(vis0.view(np.int32).copy()).cuda()
+        c.draw_cull_first_pass(v, dvis, t)
+        assert c.check() == 0
+        assert_records_equal(t.read(), O.cull(1, v, edited, vis=vis0.copy())[:2], "pass 1, bound rows")
+        c.draw_cull_occlusion_pass(v, dvis, pyr, t)
+        assert c.check() == 0
+        ovis = vis0.copy()
+        n2, recs2, _ = O.cull(2, v, edited, vis=ovis, pyramid=opyr)
+        assert_records_equal(t.read(), (n2, recs2), "pass 2, bound rows")
+        assert np.array_equal(dvis.cpu().numpy().view(np.uint32), ovis)
+    finally:
+        c.bind_dynamic_transforms(None)
+    t = Target.alloc(sc.count)
+    c.draw_cull(v, t)
+    assert c.check() == 0
+    assert_records_equal(t.read(), O.cull(0, v, sc)[:2], "frustum after unbinding")
+
+
+def test_bound_dynamic_rows_in_batch_rotate_and_clusters(stress_ctx, cluster_ctx):
+    c, sc = stress_ctx
+    n = 700
+    rows = _moved_rows(sc, n, 22)
+    bound = torch.from_numpy(rows.view(np.float32).reshape(-1).copy()).pin_memory()
+    edited = S.Scene(sc.objects, sc.transforms.copy(), sc.surfaces, sc.lods)
+    edited.transforms[:n] = rows
+    c.bind_dynamic_transforms(bound)
+    try:
+        # a batch of frustum views reads the bound rows too
+        views, keep, ref = _batch(c, sc, n_views=4, seed=23, mode=abi.MODE_FRUSTUM)
+        abi.check(abi.load().blz_cull_batch(c.ctx, views, len(ref), None), "blz_cull_batch")
+        assert c.check() == 0
+        for i, (v, objs, _, t) in enumerate(ref):
+            assert_records_equal(t.read(), O.cull(0, v, edited, objects=objs)[:2], f"batch view {i}, bound rows")
+        # rotation starts from the bound row for ids below the bound count
+        ids = np.array([3, 650, 699, 5000], np.uint32)
+        axes = np.tile(np.array([[0.0, 0.0, 1.0]], np.float32), (4, 1))
+        dst = torch.zeros(4 * 8, dtype=torch.float32, device="cuda")
+        c.rotate_transforms(torch.from_numpy(ids.view(np.int32).copy()).cuda(), torch.from_numpy(axes.reshape(-1)).cuda(),
+                            0.25, dst)
+        assert c.check() == 0
+        want = O.transforms_rotate(edited.transforms, ids, axes, 0.25)
+        assert np.array_equal(dst.cpu().numpy().view(np.uint32), want.view(np.uint32).reshape(-1))
+    finally:
+        c.bind_dynamic_transforms(None)
+    # the cluster cull of another context
+    cc, csc = cluster_ctx
+    crows = _moved_rows(csc, 300, 24)
+    cedit = S.Scene(csc.objects, csc.transforms.copy(), csc.surfaces, csc.lods, clusters=csc.clusters)
+    cedit.transforms[:300] = crows
+    cb = torch.from_numpy(crows.view(np.float32).reshape(-1).copy()).pin_memory()
+    v = view_for(zfar=1e4, position=(0.0, 0.0, -50.0))
+    cap = O._cluster_upper_bound(csc, csc.objects)
+    cc.bind_dynamic_transforms(cb)
+    try:
+        t = Target.alloc(cap)
+        cc.cluster_cull(v, t)
+        assert cc.check() == 0
+        n, recs, _, _ = O.cull_clusters(v, cedit, capacity=cap)
+        assert_records_equal(t.read(), (n, recs), "clusters, bound rows")
+    finally:
+        cc.bind_dynamic_transforms(None)
+
+
+def test_bind_dynamic_argument_checks(stress_ctx):
+    c, sc = stress_ctx
+    rows = torch.zeros((len(sc.transforms) + 1) * 8, dtype=torch.float32, device="cuda")
+    with pytest.raises(abi.BlzError):
+        c.bind_dynamic_transforms(rows)  # more rows than the scene has transforms
+    with pytest.raises(abi.BlzError):
+        c.bind_dynamic_transforms(rows[4:12])  # not 32-byte aligned
+    c.bind_dynamic_transforms(None)
