@@ -580,7 +580,7 @@ int blz_cull_instanced(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList 
         rc = ensure_chunk_scratch(c, chunks, tile);
         if (rc != BLZ_OK) return rc;
         const uint32_t groups = instanced_group_count(chunks);
-        const size_t words = static_cast<size_t>(groups) * nL + nL;
+        const size_t words = static_cast<size_t>(groups) * nL + nL + 1;  // counts, totals, finished-block counter
         if (words > c->instWords) {
             if (c->capturing) return fail(BLZ_ERR_CAPACITY, "scratch must grow, which a capture cannot record: run the call once before capturing");
             if (c->instScratch) {
@@ -614,6 +614,7 @@ int blz_cull_instanced(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList 
         q.nL = nL;
         q.hist = c->instScratch;
         q.totals = c->instScratch + static_cast<size_t>(groups) * nL;
+        q.done = q.totals + nL;
         q.lods = c->scene.lods;
         q.counters = counters;
         q.instances = instances;

@@ -568,15 +568,20 @@ cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t thre
 // The instanced cull (drawInstCountReset + drawInstCull + drawInstCmd) decides exactly what the
 // frustum + LOD pass decides: every visible object and its LOD. So it runs the FRUSTUM decide
 // kernel, whose staged (objectId, lodId) records are in object order per chunk, and then turns
-// them into per-LOD instance lists with a stable counting sort over groups of kInstGroup chunks:
+// them into per-LOD instance lists with a stable counting sort over groups of kInstGroup chunks.
+// The group counts are kept LOD-major (hist[lod * groups + group]) so that one LOD's counts are
+// contiguous:
 //   count    per group, the number of records of each LOD (shared-memory histogram);
-//   offsets  per LOD, an exclusive scan of the group counts (one warp per LOD) and the total;
-//   place    per group, each warp counts its chunk's records per LOD, the block scans those rows
+//   offsets  one warp per LOD loads all of that LOD's group counts at once, scans them into
+//            exclusive offsets and writes the LOD's total; the block that finishes last writes the
+//            counters and, in ascending LOD order, one command per non-empty LOD;
+//   place    per group, the group's offset in each LOD's list and the LODs' instanceOffsets are
+//            staged in shared memory while each warp counts its chunk's records per LOD; the block scans those rows
 //            per LOD, and each warp places its records in order (ranks inside 32-record slices
-//            from __match_any_sync); block 0 writes the counters and, in ascending LOD order, one
-//            command per non-empty LOD.
+//            from __match_any_sync).
 
 constexpr uint32_t kInstGroup = 32;  // chunks per group, one warp each
+constexpr uint32_t kInstOffPer = 4;  // group counts per lane per round of the offsets scan
 
 __global__ void __launch_bounds__(kInstGroup * 32) inst_count_kernel(const InstStagedParams q) {
     extern __shared__ uint32_t s_hist[];  // [nL]
@@ -591,52 +596,152 @@ __global__ void __launch_bounds__(kInstGroup * 32) inst_count_kernel(const InstS
         for (uint32_t j = lane; j < n; j += 32) atomicAdd(&s_hist[__ldcg(st + j).y], 1u);
     }
     __syncthreads();
-    uint32_t* h = q.hist + static_cast<size_t>(blockIdx.x) * nL;
-    for (uint32_t b = threadIdx.x; b < nL; b += kInstGroup * 32) h[b] = s_hist[b];
+    for (uint32_t b = threadIdx.x; b < nL; b += kInstGroup * 32) q.hist[static_cast<size_t>(b) * q.groups + blockIdx.x] = s_hist[b];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *q.done = 0u;  // the offsets launch's finished-block counter
 }
 
 __global__ void __launch_bounds__(1024) inst_offsets_kernel(const InstStagedParams q) {
+    __shared__ uint32_t s_warpSums[32];
+    __shared__ uint32_t s_last;
+    __shared__ unsigned int s_flags;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t b = blockIdx.x * 32u + warp;
-    if (b >= q.nL) return;
-    uint32_t run = 0;
-    for (uint32_t g0 = 0; g0 < q.groups; g0 += 32u) {
-        const uint32_t g = g0 + lane;
-        const uint32_t x = g < q.groups ? __ldcg(q.hist + static_cast<size_t>(g) * q.nL + b) : 0u;
-        uint32_t incl = x;
+    if (b < q.nL) {
+        uint32_t* h = q.hist + static_cast<size_t>(b) * q.groups;
+        uint32_t run = 0;
+        for (uint32_t g0 = 0; g0 < q.groups; g0 += 32u * kInstOffPer) {
+            // lane L holds groups g0 + L*kInstOffPer .. +kInstOffPer-1 (all loads issued together)
+            uint32_t x[kInstOffPer];
+            uint32_t mine = 0;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= static_cast<uint32_t>(o)) incl += n;
+            for (uint32_t k = 0; k < kInstOffPer; ++k) {
+                const uint32_t g = g0 + lane * kInstOffPer + k;
+                x[k] = g < q.groups ? __ldcg(h + g) : 0u;
+                mine += x[k];
+            }
+            uint32_t incl = mine;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= static_cast<uint32_t>(o)) incl += n;
+            }
+            uint32_t at = run + incl - mine;
+#pragma unroll
+            for (uint32_t k = 0; k < kInstOffPer; ++k) {
+                const uint32_t g = g0 + lane * kInstOffPer + k;
+                if (g < q.groups) h[g] = at;
+                at += x[k];
+            }
+            run += __shfl_sync(0xFFFFFFFFu, incl, 31);
         }
-        if (g < q.groups) q.hist[static_cast<size_t>(g) * q.nL + b] = run + incl - x;
-        run += __shfl_sync(0xFFFFFFFFu, incl, 31);
+        if (lane == 0) q.totals[b] = run;
     }
-    if (lane == 0) q.totals[b] = run;
+    // the block that finishes last (threadfence reduction: a counter, no waiting) writes the
+    // counters and, in ascending LOD order, one command per non-empty LOD
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(q.done, 1u) == gridDim.x - 1u ? 1u : 0u;
+        s_flags = 0u;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const uint32_t nL = q.nL;
+    const uint32_t slots = q.slotsPerLod ? q.slotsPerLod : 0xFFFFFFFFu;
+    const uint32_t per = (nL + 1023u) / 1024u;
+    const uint32_t b0 = min(nL, threadIdx.x * per), b1 = min(nL, b0 + per);
+    uint32_t mine = 0;
+    for (uint32_t l = b0; l < b1; ++l) mine += __ldcg(q.totals + l) ? 1u : 0u;
+    uint32_t incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += x;
+    }
+    if (lane == 31) s_warpSums[warp] = incl;
+    __syncthreads();
+    uint32_t warpOff = 0, all = 0;
+    for (uint32_t w = 0; w < 32u; ++w) {
+        if (w < warp) warpOff += s_warpSums[w];
+        all += s_warpSums[w];
+    }
+    uint32_t out = warpOff + incl - mine;
+    unsigned int f = 0u;
+    for (uint32_t l = b0; l < b1; ++l) {
+        const uint32_t total = __ldcg(q.totals + l);
+        q.counters[l].instanceCount = total;
+        const uint32_t offset = __ldg(&q.counters[l].instanceOffset);
+        if (total > slots || static_cast<uint64_t>(offset) + min(total, slots) > q.instanceCapacity)
+            f |= BLZ_FLAG_INSTANCE_OVERFLOW;
+        if (total == 0u) continue;
+        if (out < q.capacity) {
+            uint32_t* w = reinterpret_cast<uint32_t*>(q.cmds + static_cast<size_t>(out) * q.stride);
+            const uint2 lod = __ldg(reinterpret_cast<const uint2*>(q.lods + l));  // indexCount, firstIndex
+            w[0] = offset;
+            w[1] = lod.x;
+            w[2] = min(total, slots);
+            w[3] = lod.y;
+            w[4] = 0u;
+            w[5] = 0u;
+        }
+        ++out;
+    }
+    if (all > q.capacity) f |= BLZ_FLAG_COMMAND_OVERFLOW;
+    if (f) atomicOr(&s_flags, f);
+    if (threadIdx.x == 0) *q.drawCount = all;
+    __syncthreads();
+    if (threadIdx.x == 0 && s_flags) atomicOr(q.status, s_flags);
 }
 
+constexpr uint32_t kInstBatch = 4;  // 32-record slices whose loads are issued together
+
 __global__ void __launch_bounds__(kInstGroup * 32) inst_place_kernel(const InstStagedParams q) {
-    extern __shared__ uint32_t s_rows[];  // [kInstGroup][nL]: per-warp counts, then offsets
-    __shared__ uint32_t s_warpSums[kInstGroup];
+    // [kInstGroup][nL] per-warp counts, then offsets; [nL] the group's offset in each LOD's list;
+    // [nL] each LOD's instanceOffset
+    extern __shared__ uint32_t s_rows[];
     __shared__ unsigned int s_flags;
     const uint32_t nL = q.nL;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    uint32_t* s_goff = s_rows + kInstGroup * nL;
+    uint32_t* s_ioff = s_goff + nL;
+    const uint32_t chunk = blockIdx.x * kInstGroup + warp;
+    const uint32_t n = chunk < q.totalTiles ? __ldcg(q.chunkCount + chunk) : 0u;
+    const uint2* st = q.staged + static_cast<size_t>(chunk) * q.chunkSize;
+    auto load_batch = [&](uint32_t j0, uint2 (&r)[kInstBatch]) {
+#pragma unroll
+        for (uint32_t k = 0; k < kInstBatch; ++k) {
+            const uint32_t j = j0 + k * 32u + lane;
+            r[k] = j < n ? __ldcg(st + j) : make_uint2(0u, 0xFFFFFFFFu);
+        }
+    };
+    uint2 first[kInstBatch];  // the chunk's first 128 records, loaded once for both walks
+    load_batch(0, first);
+    for (uint32_t b = threadIdx.x; b < nL; b += kInstGroup * 32) {
+        s_goff[b] = __ldcg(q.hist + static_cast<size_t>(b) * q.groups + blockIdx.x);
+        s_ioff[b] = __ldg(&q.counters[b].instanceOffset);
+    }
     for (uint32_t j = threadIdx.x; j < kInstGroup * nL; j += kInstGroup * 32) s_rows[j] = 0u;
     if (threadIdx.x == 0) s_flags = 0u;
     __syncthreads();
-    const uint32_t chunk = blockIdx.x * kInstGroup + warp;
-    const bool have = chunk < q.totalTiles;
-    const uint32_t n = have ? __ldcg(q.chunkCount + chunk) : 0u;
-    const uint2* st = q.staged + static_cast<size_t>(chunk) * q.chunkSize;
     uint32_t* row = s_rows + warp * nL;
     const uint32_t lt = lanemask_lt();
     // 1. this chunk's records per LOD (only this warp touches its row)
-    for (uint32_t j0 = 0; j0 < n; j0 += 32u) {
-        const uint32_t j = j0 + lane;
-        const uint32_t b = j < n ? __ldcg(st + j).y : 0xFFFFFFFFu;
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
-        if (b != 0xFFFFFFFFu && (peers & lt) == 0u) row[b] += __popc(peers);
-        __syncwarp();
+    for (uint32_t j0 = 0; j0 < n; j0 += 32u * kInstBatch) {
+        uint2 r[kInstBatch];
+        if (j0 == 0) {
+#pragma unroll
+            for (uint32_t k = 0; k < kInstBatch; ++k) r[k] = first[k];
+        } else {
+            load_batch(j0, r);
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kInstBatch; ++k) {
+            const uint32_t b = r[k].y;
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
+            if (b != 0xFFFFFFFFu && (peers & lt) == 0u) row[b] += __popc(peers);
+            __syncwarp();
+        }
     }
     __syncthreads();
     // 2. per LOD, exclusive offsets of the warps' chunks inside the group
@@ -650,71 +755,34 @@ __global__ void __launch_bounds__(kInstGroup * 32) inst_place_kernel(const InstS
     }
     __syncthreads();
     // 3. place the records in object order
-    const uint32_t* groupBase = q.hist + static_cast<size_t>(blockIdx.x) * nL;
     const uint32_t slots = q.slotsPerLod ? q.slotsPerLod : 0xFFFFFFFFu;
     unsigned int flags = 0u;
-    for (uint32_t j0 = 0; j0 < n; j0 += 32u) {
-        const uint32_t j = j0 + lane;
-        const uint2 rec = j < n ? __ldcg(st + j) : make_uint2(0u, 0xFFFFFFFFu);
-        const uint32_t b = rec.y;
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
-        uint32_t before = 0;
-        if (b != 0xFFFFFFFFu) before = row[b];
-        __syncwarp();
-        if (b != 0xFFFFFFFFu) {
-            if ((peers & lt) == 0u) row[b] = before + __popc(peers);
-            const uint32_t pos = __ldcg(groupBase + b) + before + __popc(peers & lt);
-            const uint64_t at = static_cast<uint64_t>(__ldg(&q.counters[b].instanceOffset)) + pos;
-            if (pos < slots && at < q.instanceCapacity) q.instances[at] = rec.x;
-            else flags |= BLZ_FLAG_INSTANCE_OVERFLOW;
+    for (uint32_t j0 = 0; j0 < n; j0 += 32u * kInstBatch) {
+        uint2 r[kInstBatch];
+        if (j0 == 0) {
+#pragma unroll
+            for (uint32_t k = 0; k < kInstBatch; ++k) r[k] = first[k];
+        } else {
+            load_batch(j0, r);
         }
-        __syncwarp();
+#pragma unroll
+        for (uint32_t k = 0; k < kInstBatch; ++k) {
+            const uint32_t b = r[k].y;
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
+            uint32_t before = 0;
+            if (b != 0xFFFFFFFFu) before = row[b];
+            __syncwarp();
+            if (b != 0xFFFFFFFFu) {
+                if ((peers & lt) == 0u) row[b] = before + __popc(peers);
+                const uint32_t pos = s_goff[b] + before + __popc(peers & lt);
+                const uint64_t at = static_cast<uint64_t>(s_ioff[b]) + pos;
+                if (pos < slots && at < q.instanceCapacity) q.instances[at] = r[k].x;
+                else flags |= BLZ_FLAG_INSTANCE_OVERFLOW;
+            }
+            __syncwarp();
+        }
     }
     if (flags) atomicOr(&s_flags, flags);
-    // 4. block 0: counters and one command per non-empty LOD, in ascending LOD order
-    if (blockIdx.x == 0) {
-        const uint32_t per = (nL + kInstGroup * 32 - 1) / (kInstGroup * 32);
-        const uint32_t b0 = min(nL, threadIdx.x * per), b1 = min(nL, b0 + per);
-        uint32_t mine = 0;
-        for (uint32_t b = b0; b < b1; ++b) mine += __ldcg(q.totals + b) ? 1u : 0u;
-        uint32_t incl = mine;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= static_cast<uint32_t>(o)) incl += x;
-        }
-        if (lane == 31) s_warpSums[warp] = incl;
-        __syncthreads();
-        uint32_t warpOff = 0, all = 0;
-        for (uint32_t w = 0; w < kInstGroup; ++w) {
-            if (w < warp) warpOff += s_warpSums[w];
-            all += s_warpSums[w];
-        }
-        uint32_t out = warpOff + incl - mine;
-        unsigned int f = 0u;
-        for (uint32_t b = b0; b < b1; ++b) {
-            const uint32_t total = __ldcg(q.totals + b);
-            q.counters[b].instanceCount = total;
-            const uint32_t offset = __ldg(&q.counters[b].instanceOffset);
-            if (total > slots || static_cast<uint64_t>(offset) + min(total, slots) > q.instanceCapacity)
-                f |= BLZ_FLAG_INSTANCE_OVERFLOW;
-            if (total == 0u) continue;
-            if (out < q.capacity) {
-                uint32_t* w = reinterpret_cast<uint32_t*>(q.cmds + static_cast<size_t>(out) * q.stride);
-                const uint2 lod = __ldg(reinterpret_cast<const uint2*>(q.lods + b));  // indexCount, firstIndex
-                w[0] = offset;
-                w[1] = lod.x;
-                w[2] = min(total, slots);
-                w[3] = lod.y;
-                w[4] = 0u;
-                w[5] = 0u;
-            }
-            ++out;
-        }
-        if (all > q.capacity) f |= BLZ_FLAG_COMMAND_OVERFLOW;
-        if (f) atomicOr(&s_flags, f);
-        if (threadIdx.x == 0) *q.drawCount = all;
-    }
     __syncthreads();
     if (threadIdx.x == 0 && s_flags) atomicOr(q.status, s_flags);
 }
@@ -732,7 +800,7 @@ cudaError_t launch_instanced_staged(const PipeParams& p, const InstStagedParams&
     else e = launch_decide_t<BLZ_MODE_FRUSTUM, true, kObjThreads, kObjOpt>(p, 0, smCount, s);
     if (e != cudaSuccess) return e;
     const size_t histBytes = sizeof(uint32_t) * q.nL;
-    const size_t rowBytes = sizeof(uint32_t) * kInstGroup * q.nL;
+    const size_t rowBytes = sizeof(uint32_t) * (kInstGroup + 2) * q.nL;
     if (rowBytes > 48 * 1024) {
         e = cudaFuncSetAttribute(inst_place_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(rowBytes));
         if (e != cudaSuccess) return e;

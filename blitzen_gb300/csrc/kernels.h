@@ -117,6 +117,7 @@ struct InstStagedParams {
     uint32_t groups, nL;        // chunk groups of the counting sort, LOD count
     uint32_t* hist;             // scratch [groups * nL]: group counts, then exclusive offsets
     uint32_t* totals;           // scratch [nL]
+    uint32_t* done;             // scratch: offsets blocks that finished
     const BlzLodData* lods;
     BlzLodInstanceCounter* counters;
     uint32_t* instances;
@@ -197,7 +198,7 @@ bool batch_shape_supported(uint32_t threads, uint32_t opt);
 cudaError_t launch_batch_cull(const PipeParams& p, uint32_t threads, uint32_t opt, uint32_t blocksPerSm, int smCount,
                               cudaStream_t s);
 uint32_t instanced_tile_size();
-constexpr uint32_t kInstStagedMaxLods = 1024;  // the staged instanced path keeps [32][LODs] counts in shared memory
+constexpr uint32_t kInstStagedMaxLods = 1024;  // the staged instanced path keeps [34][LODs] words in shared memory
 uint32_t instanced_group_count(uint32_t chunks);
 cudaError_t launch_instanced_staged(const PipeParams& p, const InstStagedParams& q, uint32_t threads, uint32_t opt,
                                     int smCount, cudaStream_t s);
