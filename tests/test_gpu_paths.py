@@ -544,3 +544,41 @@ def test_bind_dynamic_argument_checks(stress_ctx):
     with pytest.raises(abi.BlzError):
         c.bind_dynamic_transforms(rows[4:12])  # not 32-byte aligned
     c.bind_dynamic_transforms(None)
+
+
+def test_cluster_object_stage_matches_the_pinned_frustum_lod_path(lib):
+    """With every cluster test made to pass (huge cluster spheres, open cones, no pyramid), the
+    cluster cull emits exactly the chosen LOD's cluster range of every object the frustum + LOD cull
+    emits: the cluster path's object stage agrees with the path pinned to the reference shaders."""
+    sc = S.cluster_scene(6000, seed=7, clusters_per_mesh=60)
+    sc.clusters["radius"] = 1e6
+    sc.clusters["coneAxis"] = 0       # a zero axis never passes the cutoff (an int8 axis can be
+    sc.clusters["coneCutoff"] = 127   # a little longer than 1, so cutoff 1.0 alone does not open it)
+    c = Culler(0)
+    try:
+        c.setup_for_rendering(sc)
+        v = view_for(zfar=1e4, position=(0.0, 0.0, -50.0))
+        t = Target.alloc(sc.count)
+        c.draw_cull(v, t)
+        assert c.check() == 0
+        n, recs = t.read()
+        assert n > 100
+        want_obj, want_ids = [], []
+        for rec in recs:
+            s = sc.surfaces[sc.objects[rec[0]]["surfaceId"]]
+            lods = sc.lods[int(s["lodOffset"]):int(s["lodOffset"]) + int(s["lodCount"])]
+            k = int(np.flatnonzero((lods["firstIndex"] == rec[3]) & (lods["indexCount"] == rec[1]))[0])
+            off, cnt = int(lods[k]["clusterOffset"]), int(lods[k]["clusterCount"])
+            want_obj += [int(rec[0])] * cnt
+            want_ids += list(range(off, off + cnt))
+        cap = len(want_ids) + 10
+        ct = Target.alloc(cap)
+        ids = torch.zeros(cap, dtype=torch.int32, device="cuda")
+        c.cluster_cull(v, ct, cluster_ids=ids)
+        assert c.check() == 0
+        m, crecs = ct.read()
+        assert m == len(want_ids)
+        assert np.array_equal(crecs[:, 0], np.array(want_obj, np.uint32))
+        assert np.array_equal(ids[:m].cpu().numpy().view(np.uint32), np.array(want_ids, np.uint32))
+    finally:
+        c.close()
