@@ -130,6 +130,14 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
                                                     const SurfaceCache& surf, unsigned int& flags) {
     constexpr uint32_t STEP = 32u * OPT;
     constexpr bool PACK = (MODE == BLZ_MODE_FIRST) && SINGLE;  // candidate ring of 2 * STEP entries
+    // Single-view pass 2 walks its chunk from the last object down: pass 1 walked the same chunk
+    // upwards just before (with only the pyramid build between), so the lines it touched last are
+    // the ones still in L2. Records are then staged in descending order; the scatter writes each
+    // chunk's records back to front. Slot i of the walk is object `walk(i)`; past the end it is
+    // kNoObject, never active.
+    constexpr bool DOWN = (MODE == BLZ_MODE_LATE) && SINGLE;
+    constexpr uint32_t kNoObject = 0xFFFFFFFFu;
+    auto walk = [&](uint32_t i) -> uint32_t { return i < limit ? (DOWN ? base + limit - 1u - i : i) : kNoObject; };
     const uint32_t lane = threadIdx.x & 31u;
     if (sc.transformCount == 0u || sc.surfaceCount == 0u) {
         // nothing can be looked up: every object of the pass has a bad id and none is visible
@@ -209,8 +217,8 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
     auto prefetch = [&](uint32_t at) {
 #pragma unroll
         for (int k = 0; k < OPT; ++k) {
-            const uint32_t i = at + k * 32u + lane;
-            const bool in = i < limit;
+            const uint32_t i = walk(at + k * 32u + lane);
+            const bool in = i != kNoObject;
             nro[k] = in ? __ldg(reinterpret_cast<const uint2*>(bv.objects) + i) : make_uint2(0u, 0u);
             nvis[k] = in ? 1u : 0u;
             if (MODE == BLZ_MODE_FIRST && in) nvis[k] = __ldg(bv.vis + i);
@@ -246,7 +254,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
         for (int k = 0; k < OPT; ++k) {
             ro[k] = nro[k];
             vis[k] = nvis[k];  // pass 1: active when visible last frame (drawOccFirst.cs.hlsl:22-25)
-            obj[k] = sb + k * 32u + lane;
+            obj[k] = DOWN ? walk(sb + k * 32u + lane) : sb + k * 32u + lane;
         }
         if constexpr (PACK) {
             if (sb + STEP < limit) prefetch(sb + STEP);
@@ -453,14 +461,20 @@ __global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const 
     if (myChunk >= p.totalTiles) return;
     const uint32_t base = s_base[warp];
     const BatchViewDev& bv = view_of<SINGLE>(p, s_vi[warp]);
+    // staged record i goes to slot base + i, or base + n - 1 - i for a chunk staged last object first
+    const bool down = SINGLE && p.descending != 0u;
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
         const uint32_t i = lane + 32u * u;
-        if (i < myN && base + i < bv.capacity) put_record(bv.cmds, bv.stride, base + i, pre[u].x, preLod[u].x, preLod[u].y);
+        const uint32_t slot = base + (down ? myN - 1u - i : i);
+        if (i < myN && slot < bv.capacity) put_record(bv.cmds, bv.stride, slot, pre[u].x, preLod[u].x, preLod[u].y);
     }
     for (uint32_t i = lane + 64u; i < myN; i += 32) {
-        const uint32_t slot = base + i;
-        if (slot >= bv.capacity) break;
+        const uint32_t slot = base + (down ? myN - 1u - i : i);
+        if (slot >= bv.capacity) {
+            if (down) continue;
+            break;
+        }
         const uint2 rec = __ldcg(myStage + i);
         const uint2 lod = __ldg(reinterpret_cast<const uint2*>(p.sc.lods + rec.y));  // indexCount, firstIndex
         put_record(bv.cmds, bv.stride, slot, rec.x, lod.x, lod.y);
@@ -554,11 +568,13 @@ static cudaError_t launch_single_mode(const PipeParams& p, uint32_t threads, uin
 
 cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t threads, uint32_t opt, int smCount,
                                cudaStream_t s) {
+    PipeParams q = p;
+    q.descending = mode == BLZ_MODE_LATE ? 1u : 0u;  // the single-view pass-2 decide walks its chunks downwards
     switch (mode) {
-        case BLZ_MODE_FRUSTUM: return launch_single_mode<BLZ_MODE_FRUSTUM>(p, threads, opt, smCount, s);
-        case BLZ_MODE_FIRST: return launch_single_mode<BLZ_MODE_FIRST>(p, threads, opt, smCount, s);
-        case BLZ_MODE_LATE: return launch_single_mode<BLZ_MODE_LATE>(p, threads, opt, smCount, s);
-        case BLZ_MODE_TEMPORAL: return launch_single_mode<BLZ_MODE_TEMPORAL>(p, threads, opt, smCount, s);
+        case BLZ_MODE_FRUSTUM: return launch_single_mode<BLZ_MODE_FRUSTUM>(q, threads, opt, smCount, s);
+        case BLZ_MODE_FIRST: return launch_single_mode<BLZ_MODE_FIRST>(q, threads, opt, smCount, s);
+        case BLZ_MODE_LATE: return launch_single_mode<BLZ_MODE_LATE>(q, threads, opt, smCount, s);
+        case BLZ_MODE_TEMPORAL: return launch_single_mode<BLZ_MODE_TEMPORAL>(q, threads, opt, smCount, s);
         default: return cudaErrorInvalidValue;
     }
 }

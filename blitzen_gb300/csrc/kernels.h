@@ -85,7 +85,7 @@ struct PipeParams {
     uint32_t viewCount;
     uint32_t totalTiles;   // chunks over all views
     uint32_t chunkSize;    // objects per chunk, a multiple of 32
-    uint32_t pad0;
+    uint32_t descending;   // single-view pass 2: chunks were walked and staged last object first
     Scratch* scratch;      // status word
     uint2* staged;         // [totalTiles * chunkSize] (objectId, lodId)
     uint32_t* chunkCount;  // [totalTiles]
