@@ -81,15 +81,21 @@ def _time(fn, reps, stream):
     return float(np.median(out))
 
 
-def batched_views(culler, scene, device, n_views=64, reps=20) -> dict:
+def batched_views(culler, scene, device, n_views=64, reps=20, shape=None) -> dict:
+    """64 views of log-uniform size over the resident scene: one batched launch (and its graph)
+    against one launch per view. shape = (threads, objects per thread, blocks per SM) fixes the
+    launch shape; by default the autotuner picks it."""
     lib = abi.load()
     views, keep, total = build_views(culler, scene, device, n_views)
     stream = torch.cuda.current_stream(device)
     sp = C.c_void_p(stream.cuda_stream)
 
-    # autotuned launch shape for this batch
     best, us = abi.LaunchShape(), C.c_float(0)
-    abi.check(lib.blz_autotune_batch(culler.ctx, views, n_views, 3, sp, C.byref(best), C.byref(us)), "autotune")
+    if shape is None:  # autotuned launch shape for this batch
+        abi.check(lib.blz_autotune_batch(culler.ctx, views, n_views, 3, sp, C.byref(best), C.byref(us)), "autotune")
+    else:
+        best = abi.LaunchShape(shape[0], shape[1], shape[2], 0)
+        abi.check(lib.blz_set_launch_shape(culler.ctx, C.byref(best)), "launch shape")
 
     # parity: batched == per-view, record by record, before timing anything
     abi.check(lib.blz_cull_batch(culler.ctx, views, n_views, sp), "batch")

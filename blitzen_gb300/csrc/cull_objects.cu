@@ -46,6 +46,23 @@ __device__ __forceinline__ uint32_t find_view(const uint32_t* tileStart, uint32_
     return lo;
 }
 
+// The same for a chunk index c that is equal on every lane of the warp: a 32-ary search, one round
+// of loads per factor of 32 views instead of one dependent load per halving.
+__device__ __forceinline__ uint32_t find_view_warp(const uint32_t* tileStart, uint32_t nViews, uint32_t c) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t lo = 0, n = nViews;  // the view is in [lo, lo + n), and tileStart[lo] <= c
+    while (n > 1u) {
+        const uint32_t step = (n + 31u) >> 5;
+        const uint32_t cand = lo + lane * step;
+        const bool le = cand < lo + n && __ldg(tileStart + cand) <= c;
+        const uint32_t k = 31u - static_cast<uint32_t>(__clz(static_cast<int>(__ballot_sync(0xFFFFFFFFu, le))));
+        const uint32_t end = lo + n;
+        lo += k * step;
+        n = min(step, end - lo);
+    }
+    return lo;
+}
+
 // ------------------------------------------------------------------ decisions
 
 constexpr uint32_t kChunk = 512;  // objects per chunk of batched views (single views size theirs)
@@ -342,7 +359,7 @@ __global__ void __launch_bounds__(THREADS, SINGLE ? 1024 / THREADS : 1) cull_dec
         const uint32_t next = next_chunk(chunk);  // asked now, used after this chunk
         uint32_t vi = 0, first = 0;
         if constexpr (!SINGLE) {
-            vi = find_view(p.tileStart, p.viewCount, chunk);
+            vi = find_view_warp(p.tileStart, p.viewCount, chunk);
             first = __ldg(p.tileStart + vi);
         }
         const BatchViewDev& bv = view_of<SINGLE>(p, vi);
@@ -388,7 +405,7 @@ __global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const 
     const uint32_t c0 = blockIdx.x * kScatterChunks;
     if (blockIdx.x == 0 && threadIdx.x == 0 && p.workCounter != nullptr) *p.workCounter = 0u;
     if (c0 >= p.totalTiles) return;
-    const uint32_t vi0 = SINGLE ? 0u : find_view(p.tileStart, p.viewCount, c0);
+    const uint32_t vi0 = SINGLE ? 0u : find_view_warp(p.tileStart, p.viewCount, c0);
     const uint32_t viewStart0 = SINGLE ? 0u : __ldg(p.tileStart + vi0);
     // 0. each warp fetches its chunk's first 2 * 32 staged records and their LODs now, so those
     //    loads overlap the offset computation below
@@ -424,8 +441,15 @@ __global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const 
         uint32_t vi = vi0;
         bool starts = false;  // this chunk starts a view (the scan restarts here)
         if constexpr (!SINGLE) {
+            // the next 32 view starts after vi0: a lane's view is vi0 + those at or before its chunk
+            const uint32_t j = vi0 + 1u + lane;
+            const uint32_t sj = j < p.viewCount ? __ldg(p.tileStart + j) : 0xFFFFFFFFu;
+            uint32_t cnt = 0;
+#pragma unroll
+            for (int t = 0; t < 32; ++t) cnt += __shfl_sync(0xFFFFFFFFu, sj, t) <= c ? 1u : 0u;
             if (in) {
-                vi = find_view(p.tileStart, p.viewCount, c);
+                // more than 32 views (empty ones) can start inside the block's chunks: search then
+                vi = cnt < 32u ? vi0 + cnt : find_view(p.tileStart, p.viewCount, c);
                 starts = c == __ldg(p.tileStart + vi);
             }
         }
