@@ -103,6 +103,13 @@ static int ensure_batch_dev(blz_ctx* c, size_t bytes) {
     return BLZ_OK;
 }
 
+// The pass all views run, or -1 when they differ.
+static int uniform_mode(const BlzBatchView* views, uint32_t n) {
+    for (uint32_t i = 1; i < n; ++i)
+        if (views[i].mode != views[0].mode) return -1;
+    return n ? static_cast<int>(views[0].mode) : -1;
+}
+
 int run_batch(blz_ctx* c, const BlzBatchView* views, uint32_t n, cudaStream_t st) {
     if (!c || (n && !views)) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or views is NULL");
     if (n == 0) return BLZ_OK;
@@ -119,7 +126,8 @@ int run_batch(blz_ctx* c, const BlzBatchView* views, uint32_t n, cudaStream_t st
     rc = upload_views(c, d, ts, c->batchDev, st, p);
     if (rc != BLZ_OK) return rc;
     bind_chunk_scratch(c, p);
-    cudaError_t e = launch_batch_cull(p, c->shape.threadsPerBlock, c->shape.objectsPerThread, c->shape.blocksPerSm, c->smCount, st);
+    cudaError_t e = launch_batch_cull(p, c->shape.threadsPerBlock, c->shape.objectsPerThread, c->shape.blocksPerSm, c->smCount, st,
+                                      uniform_mode(views, n));
     if (e != cudaSuccess) return cuda_fail(e, "batch launch");
     c->launches += 2;  // decide + scatter
     return BLZ_OK;
@@ -320,7 +328,8 @@ int blz_batch_graph_create(blz_ctx* c, const BlzBatchView* views, uint32_t n, bl
         cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            cudaError_t le = launch_batch_cull(p, c->shape.threadsPerBlock, c->shape.objectsPerThread, c->shape.blocksPerSm, c->smCount, cap);
+            cudaError_t le = launch_batch_cull(p, c->shape.threadsPerBlock, c->shape.objectsPerThread, c->shape.blocksPerSm,
+                                               c->smCount, cap, uniform_mode(views, n));
             e = cudaStreamEndCapture(cap, &g->graph);
             if (le != cudaSuccess) e = le;
         }

@@ -319,7 +319,7 @@ __device__ __forceinline__ void put_record(uint8_t* cmds, uint32_t stride, uint3
 // ------------------------------------------------------------------ decide kernel
 
 template <int MODE, bool SINGLE, int THREADS, int OPT>
-__global__ void __launch_bounds__(THREADS, SINGLE ? 1024 / THREADS : 1) cull_decide_kernel(const PipeParams p) {
+__global__ void __launch_bounds__(THREADS, (SINGLE || MODE >= 0) ? 1024 / THREADS : 1) cull_decide_kernel(const PipeParams p) {
     constexpr int NW = THREADS / 32;
     __shared__ __align__(16) Survivor s_ring[NW][kRing];
     constexpr bool PACK = (MODE == BLZ_MODE_FIRST) && SINGLE;
@@ -857,8 +857,26 @@ bool batch_shape_supported(uint32_t threads, uint32_t opt) {
     return threads * opt <= 1024;
 }
 
+// A batch whose views all run one pass takes a kernel compiled for that pass: without the other
+// passes' code it fits 64 registers, twice the resident warps of the per-view-mode kernel (112).
+template <int MODE>
+static cudaError_t launch_batch_mode(const PipeParams& p, uint32_t threads, uint32_t blocksPerSm, int smCount,
+                                     cudaStream_t s) {
+    if (threads == 512) return launch_t<MODE, false, 512, 1>(p, blocksPerSm, smCount, s);
+    return launch_t<MODE, false, 256, 1>(p, blocksPerSm, smCount, s);
+}
+
 cudaError_t launch_batch_cull(const PipeParams& p, uint32_t threads, uint32_t opt, uint32_t blocksPerSm, int smCount,
-                              cudaStream_t s) {
+                              cudaStream_t s, int mode) {
+    if (mode >= 0 && opt == 1 && (threads == 256 || threads == 512)) {
+        switch (mode) {
+            case BLZ_MODE_FRUSTUM: return launch_batch_mode<BLZ_MODE_FRUSTUM>(p, threads, blocksPerSm, smCount, s);
+            case BLZ_MODE_FIRST: return launch_batch_mode<BLZ_MODE_FIRST>(p, threads, blocksPerSm, smCount, s);
+            case BLZ_MODE_LATE: return launch_batch_mode<BLZ_MODE_LATE>(p, threads, blocksPerSm, smCount, s);
+            case BLZ_MODE_TEMPORAL: return launch_batch_mode<BLZ_MODE_TEMPORAL>(p, threads, blocksPerSm, smCount, s);
+            default: break;
+        }
+    }
 #define BLZ_BATCH_CASE(T, O) \
     if (threads == T && opt == O) return launch_t<kModeRuntime, false, T, O>(p, blocksPerSm, smCount, s);
     BLZ_BATCH_CASE(128, 1) BLZ_BATCH_CASE(128, 2) BLZ_BATCH_CASE(128, 4) BLZ_BATCH_CASE(128, 8)

@@ -195,8 +195,9 @@ bool single_shape_supported(uint32_t threads, uint32_t opt);
 cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t threads, uint32_t opt, int smCount,
                                cudaStream_t s);
 bool batch_shape_supported(uint32_t threads, uint32_t opt);
+// mode: the pass every view of the batch runs, or -1 when they differ (the kernel reads it per view)
 cudaError_t launch_batch_cull(const PipeParams& p, uint32_t threads, uint32_t opt, uint32_t blocksPerSm, int smCount,
-                              cudaStream_t s);
+                              cudaStream_t s, int mode);
 uint32_t instanced_tile_size();
 constexpr uint32_t kInstStagedMaxLods = 1024;  // the staged instanced path keeps [34][LODs] words in shared memory
 uint32_t instanced_group_count(uint32_t chunks);

@@ -331,7 +331,10 @@ int blz_batch_graph_launch(blz_batch_graph* g, blz_stream_t stream);
 int blz_batch_graph_destroy(blz_batch_graph* g);
 
 /* Launch shape used by the batch kernel (threads per block, objects per thread, blocks per SM).
- * blz_autotune measures the candidate shapes on the given batch and keeps the fastest. */
+ * blz_set_launch_shape also sets the single-view kernels' threads and objects per thread when they
+ * have that shape (256 x 1, 2 or 4; 128 x 2 or 4; 512 x 1). blz_autotune_batch measures the
+ * candidate shapes on the given batch and keeps the fastest for the batch kernel only. A batch
+ * whose views all run the same pass uses a kernel compiled for that pass for 256 x 1 and 512 x 1. */
 typedef struct BlzLaunchShape {
     uint32_t threadsPerBlock;
     uint32_t objectsPerThread;
