@@ -127,8 +127,28 @@ int main() {
     const uint64_t hLate = fnv(recs2.data(), recs2.size() * 4);
     const uint64_t hVis = fnv(visHost.data(), visHost.size() * 4);
 
-    std::printf("frustum %u %016llx first %u late %u %016llx vis %016llx\n", n, (unsigned long long)hFrustum, n1, n2,
-                (unsigned long long)hLate, (unsigned long long)hVis);
+    // the first 4,096 transforms moved 150 units along x, bound from pinned host memory
+    const uint32_t K = 4096;
+    BlzMeshTransform* rows = nullptr;
+    if (cudaHostAlloc(reinterpret_cast<void**>(&rows), K * sizeof(BlzMeshTransform), cudaHostAllocDefault) != cudaSuccess) return 2;
+    for (uint32_t i = 0; i < K; ++i) {
+        rows[i] = tr[i];
+        rows[i].pos[0] = tr[i].pos[0] + 150.0f;
+    }
+    CHECK(blz_scene_bind_dynamic(ctx, rows, K));
+    CHECK(blz_cull_frustum(ctx, &view, all, &t, nullptr));
+    CHECK(blz_ctx_check(ctx, nullptr, &flags));
+    CHECK(blz_scene_bind_dynamic(ctx, nullptr, 0));
+    uint32_t nb = 0;
+    cudaMemcpy(&nb, count, 4, cudaMemcpyDeviceToHost);
+    std::vector<uint32_t> recsB(size_t(nb) * 6);
+    cudaMemcpy(recsB.data(), cmds, recsB.size() * 4, cudaMemcpyDeviceToHost);
+    const uint64_t hBound = fnv(recsB.data(), recsB.size() * 4);
+    cudaFreeHost(rows);
+
+    std::printf("frustum %u %016llx first %u late %u %016llx vis %016llx bound %u %016llx\n", n,
+                (unsigned long long)hFrustum, n1, n2, (unsigned long long)hLate, (unsigned long long)hVis, nb,
+                (unsigned long long)hBound);
     cudaFree(cmds);
     cudaFree(count);
     cudaFree(vis);

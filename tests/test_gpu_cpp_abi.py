@@ -1,6 +1,6 @@
 """The C ABI from a C++ caller with no Python in its process (tests/cpp/abi_smoke.cpp): the program's
 draw counts and record checksums must equal the oracle's for the same scene, built here with the
-same generator."""
+same generator, including a cull over dynamic rows bound from pinned host memory."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -82,7 +82,7 @@ def program(lib, tmp_path_factory):
 def test_cpp_caller_matches_oracle(program):
     line = subprocess.run([str(program)], check=True, capture_output=True, text=True, timeout=300).stdout.split()
     got = dict(frustum=int(line[1]), hf=int(line[2], 16), first=int(line[4]), late=int(line[6]), hl=int(line[7], 16),
-               hv=int(line[9], 16))
+               hv=int(line[9], 16), bound=int(line[11]), hb=int(line[12], 16))
     sc = _scene()
     v = O.view_setup(float(np.float32(1.2217305)), 1920.0, 1080.0, 0.1, 1e4, (0.0, 0.0, 0.0), 0.3, 0.1, 960.0, 540.0)
     n, recs, _ = O.cull(0, v, sc)
@@ -98,3 +98,9 @@ def test_cpp_caller_matches_oracle(program):
     assert got["late"] == n2
     assert got["hl"] == _fnv(recs2[:, :6].astype(np.uint32).tobytes())
     assert got["hv"] == _fnv(vis.tobytes())
+    # transforms [0, 4096) read from bound pinned rows, moved 150 units along x
+    moved = S.Scene(sc.objects, sc.transforms.copy(), sc.surfaces, sc.lods)
+    moved.transforms["pos"][:4096, 0] += np.float32(150.0)
+    nb, recsb, _ = O.cull(0, v, moved)
+    assert got["bound"] == nb and nb != n
+    assert got["hb"] == _fnv(recsb[:, :6].astype(np.uint32).tobytes())
