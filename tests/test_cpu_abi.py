@@ -139,3 +139,14 @@ def test_context_creation_without_a_device_fails_cleanly(lib):
     rc = lib.blz_ctx_create(0, C.byref(h))
     assert rc != 0 and not h.value
     assert len(lib.blz_last_error()) > 0
+
+
+def test_headers_compile_as_cpp_for_a_cpp_caller():
+    """The C++ caller (tests/cpp/abi_smoke.cpp, the reference renderer's language) compiles against
+    include/*.h: syntax only, nothing is linked or run here."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    cuda_inc = Path("/usr/local/cuda/include")
+    if not cxx or not (cuda_inc / "cuda_runtime.h").exists():
+        pytest.skip("no C++ compiler or CUDA headers")
+    subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-fsyntax-only", "-I", str(INCLUDE), "-I", str(cuda_inc),
+                    str(ROOT / "tests" / "cpp" / "abi_smoke.cpp")], check=True)
