@@ -177,9 +177,13 @@ struct blz_server {
             pending.pop_front();
         }
         if (take.empty()) return false;
+        // the requests themselves, looked up while the lock is held: submissions may insert into
+        // (and rehash) the map once it is released; running requests are never erased
+        std::vector<Request*> reqOf(take.size());
+        for (size_t k = 0; k < take.size(); ++k) reqOf[k] = reqs[take[k]].get();
         std::vector<BlzBatchView> views(take.size());
         for (size_t k = 0; k < take.size(); ++k) {
-            Request& q = *reqs[take[k]];
+            Request& q = *reqOf[k];
             q.state = ReqState::Running;
             BlzBatchView& v = views[k];
             memset(&v, 0, sizeof v);
@@ -205,7 +209,7 @@ struct blz_server {
         // rotations of the dynamic objects into each request's slab
         size_t axesAt = 0;
         for (size_t k = 0; k < take.size(); ++k) {
-            Request& q = *reqs[take[k]];
+            Request& q = *reqOf[k];
             if (!q.r.rotateCount) continue;
             memcpy(s.hostAxes + axesAt, q.axes.data(), q.axes.size() * sizeof(float));
             cudaMemcpyAsync(axes_ptr(q), s.hostAxes + axesAt, q.axes.size() * sizeof(float), cudaMemcpyHostToDevice, s.stream);
@@ -215,7 +219,7 @@ struct blz_server {
         }
         int rc = blz_cull_batch(s.ctx, views.data(), (uint32_t)views.size(), reinterpret_cast<blz_stream_t>(s.stream));
         for (size_t k = 0; k < take.size(); ++k) {
-            Request& q = *reqs[take[k]];
+            Request& q = *reqOf[k];
             cudaMemcpyAsync(&s.hostCounts[k], count_ptr(q), sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream);
             if (rc != BLZ_OK) q.status = (uint32_t)rc;
         }
