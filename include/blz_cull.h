@@ -323,7 +323,9 @@ int blz_cull_batch_per_view(blz_ctx* ctx, const BlzBatchView* views, uint32_t vi
 
 /* Captures blz_cull_batch for a fixed set of views into a CUDA graph and replays it. The views'
  * buffers must stay valid for the life of the graph; view data may be changed between replays
- * with blz_batch_graph_set_view. */
+ * with blz_batch_graph_set_view, which writes the graph's copy of the view at once (a synchronous
+ * copy): call it only when no replay of the graph is still running, as for any buffer a recorded
+ * command reads. */
 int blz_batch_graph_create(blz_ctx* ctx, const BlzBatchView* views, uint32_t viewCount,
                            blz_stream_t stream, blz_batch_graph** outGraph);
 int blz_batch_graph_set_view(blz_batch_graph* g, uint32_t viewIndex, const BlzCameraViewData* view);
