@@ -582,3 +582,46 @@ def test_cluster_object_stage_matches_the_pinned_frustum_lod_path(lib):
         assert np.array_equal(ids[:m].cpu().numpy().view(np.uint32), np.array(want_ids, np.uint32))
     finally:
         c.close()
+
+
+def test_cluster_tasks_with_vulkan_hiz(cluster_ctx):
+    """The task form against a Vulkan-form pyramid (PreviousPow2 mip 0, MIN-sampler footprint)."""
+    c, sc = cluster_ctx
+    pl, _ = abi.pyramid_layout(W, H, abi.HIZ_VULKAN)
+    v = view_for(zfar=1e4, position=(0.0, 0.0, -50.0), pw=float(pl.width), ph=float(pl.height))
+    depth = O.depth_raster(v, sc.boxes, W, H)
+    pyr = DevicePyramid(W, H, abi.HIZ_VULKAN)
+    c.generate_depth_pyramid(pyr, torch.from_numpy(depth).cuda())
+    tasks, payloads = O.cluster_tasks(v, sc, pyramid=O.pyramid_build(depth, abi.HIZ_VULKAN))
+    assert len(tasks) > 20
+    t = TaskTarget.alloc(sc.count, len(payloads) + 3)
+    c.cluster_task_cull(v, t, pyramid=pyr)
+    assert c.check() == 0
+    nt, np_, gt, gp = t.read()
+    assert (nt, np_) == (len(tasks), len(payloads))
+    assert np.array_equal(gt, tasks) and np.array_equal(gp, payloads)
+
+
+def test_instanced_with_bound_dynamic_rows(stress_ctx):
+    c, sc = stress_ctx
+    n, slots = 2000, 100_000
+    rows = _moved_rows(sc, n, 31)
+    bound = torch.from_numpy(rows.view(np.float32).reshape(-1).copy()).pin_memory()
+    edited = S.Scene(sc.objects, sc.transforms.copy(), sc.surfaces, sc.lods)
+    edited.transforms[:n] = rows
+    v = view_for(zfar=1e4)
+    ctr = O.new_counters(sc, slots)
+    cap = len(sc.lods) * slots
+    dctr = torch.from_numpy(ctr.view(np.int32).reshape(-1).copy()).cuda()
+    dinst = torch.full((cap,), -1, dtype=torch.int32, device="cuda")
+    t = Target.alloc(len(sc.lods), abi.STRIDE_D3D12)
+    c.bind_dynamic_transforms(bound)
+    try:
+        c.draw_instance_cull_pass(v, dctr, dinst, slots, t)
+        assert c.check() == 0
+    finally:
+        c.bind_dynamic_transforms(None)
+    m, cmds, octr, oinst, _ = O.cull_instanced(v, edited, ctr, cap, slots, stride=abi.STRIDE_D3D12)
+    assert_records_equal(t.read(), (m, cmds), "instanced commands, bound rows")
+    assert np.array_equal(dctr.cpu().numpy().view(np.uint32), octr.view(np.uint32).reshape(-1))
+    assert np.array_equal(dinst.cpu().numpy().view(np.uint32), oinst)
