@@ -141,37 +141,56 @@ class ClockSampler:
 
 # ----------------------------------------------------------------------------- reference arm
 
+def oracle_frame(sc, v, depth, threads):
+    """One stress frame of the oracle (the multithreaded C port of the reference's shaders) with every
+    buffer allocated beforehand: frame() restores the visibility mask, then times bo_cull pass 1,
+    bo_pyramid_build and bo_cull pass 2 alone, and returns (seconds, (n1, records1), (n2, records2),
+    pyramid, visibility)."""
+    from oracle import oracle as O
+    desc = O.scene_desc(sc)
+    out1 = np.zeros((sc.count, 6), np.uint32)
+    out2 = np.zeros((sc.count, 6), np.uint32)
+    pyr = O.HostPyramid(W, H, 0)
+    vis = sc.visibility.copy()
+    depth = np.ascontiguousarray(depth, dtype=np.float32)
+
+    def frame():
+        np.copyto(vis, sc.visibility)
+        t0 = time.perf_counter()
+        n1, r1, _ = O.cull(1, v, sc, vis=vis, threads=threads, out=out1, desc=desc)
+        O.pyramid_build(depth, into=pyr)
+        n2, r2, _ = O.cull(2, v, sc, vis=vis, pyramid=pyr, threads=threads, out=out2, desc=desc)
+        return time.perf_counter() - t0, (n1, r1), (n2, r2), pyr, vis
+
+    return frame
+
+
+def time_oracle_frames(frame, min_frames: int, seconds: float) -> list[float]:
+    """At least min_frames timed frames, more while the time budget lasts."""
+    times = []
+    t_end = time.perf_counter() + seconds
+    while len(times) < min_frames or time.perf_counter() < t_end:
+        times.append(frame()[0])
+        if len(times) >= min_frames and time.perf_counter() > t_end:
+            break
+    return times
+
+
 def run_reference(args, rank, world):
     """The CPU oracle on the full stress frame, every host thread; rank 0 only."""
     if rank != 0:
         return
-    from blitzen_gb300 import abi
     from blitzen_gb300 import scenes as S
     from oracle import oracle as O
 
     threads = os.cpu_count() or 1
     sc = S.stress_scene(args.objects, seed=args.seed)
-    v = abi.view_setup(S.fov_radians(), float(W), float(H), S.ZNEAR, 1e4, (0, 0, 0), 0, 0, W / 2, H / 2)
-    depth = O.depth_raster(v, sc.boxes, W, H)
-
-    def frame():
-        vis = sc.visibility.copy()
-        O.cull(1, v, sc, vis=vis, threads=threads)
-        p = O.pyramid_build(depth)
-        O.cull(2, v, sc, vis=vis, pyramid=p, threads=threads)
-
+    v = O.view_setup(S.fov_radians(), float(W), float(H), S.ZNEAR, S.STRESS_ZFAR, (0, 0, 0), 0, 0, W / 2, H / 2)
+    frame = oracle_frame(sc, v, O.depth_raster(v, sc.boxes, W, H), threads)
     for _ in range(max(1, min(args.warmup, 2))):
         frame()
-    steps = max(1, args.steps)
-    times = []
-    t_end = time.perf_counter() + 60.0
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        frame()
-        times.append(time.perf_counter() - t0)
-        if time.perf_counter() > t_end:
-            break
-    per = sum(times) / len(times)
+    times = time_oracle_frames(frame, max(5, args.steps), 0.0)
+    per = statistics.median(times)
     value = args.objects / per
     line = {
         "impl": "reference", "metric": "objects culled/s (4M-object two-pass occlusion frame)", "value": value,
@@ -179,7 +198,9 @@ def run_reference(args, rank, world):
         "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)", "config": workload_config(args),
         "cpu_baseline": {"value": value, "unit": "objects/s", "cores": threads, "kind": "port",
-                         "sample": f"full 4M-object frame x {len(times)} (pass 1 + pyramid + pass 2)"},
+                         "sample": f"median of {len(times)} full {args.objects}-object frames (bo_cull pass 1 + "
+                                   f"bo_pyramid_build + bo_cull pass 2; buffers preallocated, visibility "
+                                   f"restored outside the clock)"},
         "e2e": {"value": value, "unit": "objects/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -193,6 +214,31 @@ def workload_config(args):
 
 
 # ----------------------------------------------------------------------------- our arm
+
+def frame_matches(want, t1, t2, vis, pyr) -> bool:
+    """Both draw counts, every word of every record, the visibility buffer and every pyramid texel
+    equal the oracle's frame `want` = ((n1, records1), (n2, records2), pyramid words, visibility)."""
+    (n1, r1), (n2, r2), pyr_words, ovis = want
+    g1, g2 = t1.read(), t2.read()
+    ok = g1[0] == n1 and np.array_equal(g1[1], r1) and g2[0] == n2 and np.array_equal(g2[1], r2)
+    ok = ok and np.array_equal(vis.cpu().numpy().view(np.uint32), ovis)
+    ok = ok and np.array_equal(pyr.storage.cpu().numpy().view(np.uint32), pyr_words.view(np.uint32))
+    return bool(ok)
+
+
+def recorded_traffic(kernel: str, objects: int):
+    """DRAM bytes per launch of `kernel` on the stress frame from the committed ncu figures, or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            d = json.load(f)
+        e = d["kernels"][kernel]
+        if int(e["objects"]) != objects:
+            return None
+        return {"bytes_per_launch": int(e["dram_bytes_per_launch"]),
+                "source": f"ncu capture at commit {d['commit']}: {e['command']}"}
+    except Exception:
+        return None
+
 
 def main():
     args = parse()
@@ -220,7 +266,7 @@ def main():
         t_, o_ = (int(x) for x in args.shape.lower().split("x"))
         c.set_launch_shape(t_, o_)
     c.setup_for_rendering(sc)
-    v = abi.view_setup(S.fov_radians(), float(W), float(H), S.ZNEAR, 1e4, (0, 0, 0), 0, 0, W / 2, H / 2)
+    v = S.stress_view()
     depth = torch.zeros(W * H, dtype=torch.float32, device=dev)
     c.raster_boxes(v, torch.from_numpy(sc.boxes.reshape(-1)).to(dev), depth, W, H)
     vis0 = torch.from_numpy(sc.visibility.view(np.int32).copy()).to(dev)
@@ -243,6 +289,13 @@ def main():
         c.generate_depth_pyramid(pyr, depth)
         c.draw_cull_occlusion_pass(v, vis, pyr, t2)
 
+    # the oracle's answer for this frame (every host thread), the reference every check below uses
+    threads = os.cpu_count() or 1
+    hdepth_np = depth.cpu().numpy().reshape(H, W)
+    _, o1, o2, opyr, ovis = oracle_frame(sc, v, hdepth_np, threads)()
+    want = ((o1[0], o1[1].copy()), (o2[0], o2[1].copy()), opyr.data.copy(), ovis.copy())
+    exact = {}
+
     with torch.cuda.stream(side):
         for _ in range(max(args.warmup, 3)):
             vis.copy_(vis0)
@@ -251,6 +304,7 @@ def main():
         c.check()
         V1, _ = t1.read()
         V2, _ = t2.read()
+        exact["direct_calls"] = frame_matches(want, t1, t2, vis, pyr)
         # the frame as three recorded passes, replayed back to back (no host work between kernels)
         # the frame (pass 1, pyramid, pass 2) recorded once and replayed as one graph per step; the
         # three passes are also recorded one by one for the per-pass breakdown
@@ -307,6 +361,8 @@ def main():
                     flush_l2()
                     step()
                 side.synchronize()
+        # the state the last timed replay left: both record lists, the pyramid and the visibility
+        exact["timed_frame"] = frame_matches(want, t1, t2, vis, pyr)
         # per-pass breakdown (not part of the headline): each pass replayed as its own graph, and the
         # frame without pass 2 (pass 2 inside the frame = frame - that, launch overheads cancelling)
         evp = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
@@ -354,13 +410,12 @@ def main():
                     "pyramid": {"ms": t_pyr, "bytes": bytes_pyr, "GB/s": bytes_pyr / (t_pyr * 1e-3) / 1e9},
                     "frame": {"ms": t_step, "bytes": bytes_first + bytes_pyr + bytes_late,
                               "GB/s": (bytes_first + bytes_pyr + bytes_late) / (t_step * 1e-3) / 1e9}}}
-    # DRAM bytes of one pass-2 decide launch, from the ncu capture summarised in profiles/
-    prof = os.path.join(ROOT, "profiles", "cull_decide_late_4M.md")
-    if os.path.exists(prof) and args.objects == 4_000_000:
-        with open(prof) as f:
-            for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    roofline["traffic"] = int(line.split(":")[1])
+    # DRAM bytes of one pass-2 decide launch from an ncu capture (profiles/dram_traffic.json names the
+    # commit and the command it was taken with); a capture, not a measurement of this run
+    traffic = recorded_traffic("cull_decide_kernel<LATE>", args.objects)
+    if traffic:
+        roofline["traffic"] = traffic["bytes_per_launch"]
+        roofline["traffic_source"] = traffic["source"]
 
     # ---------------- e2e through the C ABI with host buffers
     hdepth = torch.empty(W * H, dtype=torch.float32, pin_memory=True)
@@ -437,11 +492,14 @@ def main():
         counts = hcounts0.numpy().copy()  # the step's result, already in host memory
         if k >= args.warmup:
             zc_ms.append(e0.elapsed_time(e1))
-    # the recorded step's counts (written to host memory) equal a direct run on the same state
-    vis.copy_(vis0)
-    step_direct()
-    torch.cuda.synchronize()
-    assert (int(counts[0]), int(counts[1])) == (t1.read()[0], t2.read()[0]), counts
+    # the last recorded step against the oracle on the scene as that step saw it (its dynamic rows)
+    edited = S.Scene(sc.objects, sc.transforms.copy(), sc.surfaces, sc.lods, visibility=sc.visibility)
+    edited.transforms[:DYNAMIC] = h_tr_np
+    _, e1_, e2_, eyr, evis = oracle_frame(edited, v, hdepth_np, threads)()
+    t1_host = Target(t1.commands, torch.from_numpy(counts[0:1].copy()), t1.stride, t1.capacity)
+    t2_host = Target(t2.commands, torch.from_numpy(counts[1:2].copy()), t2.stride, t2.capacity)
+    exact["e2e_step"] = frame_matches(((e1_[0], e1_[1]), (e2_[0], e2_[1]), eyr.data, evis), t1_host, t2_host, vis, pyr)
+    del edited
     t_e2e = max_over_ranks(sum(zc_ms) / len(zc_ms), world, dev)
     frame_zc.close()
     c.bind_dynamic_transforms(None)
@@ -478,6 +536,7 @@ def main():
             "data": "synthetic (seeded)", "config": workload_config(args), "roofline": roofline,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks.summary(),
             "wall_s_timed": wall, "draws": {"pass1": V1, "pass2": V2}, "launch_shape": c.launch_shape(),
+            "bit_exact": all(exact.values()), "bit_exact_checks": exact,
             "extras": extras,
         }
         print(json.dumps(line), flush=True)
@@ -487,25 +546,16 @@ def main():
 
 
 def cpu_baseline(sc, v, depth, seconds):
-    """The oracle (multithreaded C port of the shaders) on a bounded sample of the same frame."""
-    from oracle import oracle as O
+    """The oracle on the same full frame as the reference arm: the median of as many frames as fit in
+    `seconds` (at least 5), every host thread."""
     threads = os.cpu_count() or 1
-    n = min(sc.count, 1_000_000)
-    from blitzen_gb300.scenes import Scene
-    sub = Scene(sc.objects[:n], sc.transforms, sc.surfaces, sc.lods, visibility=sc.visibility[:n].copy())
-    p = O.pyramid_build(depth)
-    done, t0 = 0, time.perf_counter()
-    frames = 0
-    while time.perf_counter() - t0 < seconds or frames == 0:
-        vis = sub.visibility.copy()
-        O.cull(1, v, sub, vis=vis, threads=threads)
-        p = O.pyramid_build(depth)
-        O.cull(2, v, sub, vis=vis, pyramid=p, threads=threads)
-        done += n
-        frames += 1
-    dt = time.perf_counter() - t0
-    return {"value": done / dt, "unit": "objects/s", "cores": threads, "kind": "port",
-            "sample": f"{frames} frames of the first {n} objects (pass 1 + pyramid + pass 2), {dt:.1f} s"}
+    frame = oracle_frame(sc, v, depth, threads)
+    frame()
+    times = time_oracle_frames(frame, 5, seconds)
+    per = statistics.median(times)
+    return {"value": sc.count / per, "unit": "objects/s", "cores": threads, "kind": "port", "ms": per * 1e3,
+            "sample": f"median of {len(times)} full {sc.count}-object frames (bo_cull pass 1 + bo_pyramid_build + "
+                      f"bo_cull pass 2; buffers preallocated, visibility restored outside the clock)"}
 
 
 if __name__ == "__main__":

@@ -201,8 +201,9 @@ int blz_ctx_create(int device, blz_ctx** out) {
         const unsigned int one = 1u;
         e = cudaMemcpy(static_cast<char*>(c->scratchMem) + 4, &one, sizeof one, cudaMemcpyHostToDevice);
     }
-    if (e == cudaSuccess) e = cudaMalloc(&c->workCounter, sizeof(unsigned int));
-    if (e == cudaSuccess) e = cudaMemset(c->workCounter, 0, sizeof(unsigned int));
+    // word 0: the batch decide kernel's work counter; word 1: where blz_ctx_check takes the status
+    if (e == cudaSuccess) e = cudaMalloc(&c->workCounter, 2 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(c->workCounter, 0, 2 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMallocHost(&c->pinned, kPinnedBytes);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->pinnedDone, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -236,16 +237,18 @@ uint64_t blz_ctx_launch_count(const blz_ctx* c) { return c ? c->launches.load() 
 
 int blz_ctx_check(blz_ctx* c, blz_stream_t stream, uint32_t* flagsOut) {
     if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
-    cudaError_t e = cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream));
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
-    unsigned int hdr[5];
-    e = cudaMemcpy(hdr, c->scratchMem, sizeof hdr, cudaMemcpyDeviceToHost);
+    // the status word is taken and cleared in one atomic exchange on the device, so a flag that
+    // work on another stream of this context raises meanwhile is kept for the next check
+    e = launch_take_status(&c->scratch->status, c->workCounter + 1, st);
+    unsigned int hdr[2];
+    uint32_t flags = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, c->workCounter + 1, sizeof flags, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hdr, c->scratchMem, sizeof hdr, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "status read");
-    const uint32_t flags = hdr[4];
-    if (flags) {
-        unsigned int zero = 0u;
-        cudaMemcpy(static_cast<char*>(c->scratchMem) + 16, &zero, sizeof zero, cudaMemcpyHostToDevice);
-    }
     if (flags & BLZ_FLAG_TIMEOUT) {
         // a timed-out launch may have left the ticket mid-way: restart the protocol on a new epoch
         unsigned int fresh[3] = {0u, hdr[1] + 2u, 0u};

@@ -47,6 +47,7 @@ struct blz_ctx {
     uint64_t launchesAtCapture = 0;
     BlzLaunchShape shape{256, 2, 0, 0};   // batch launches
     uint32_t singleThreads = 256, singleOpt = 2;  // single-view launches
+    unsigned char* noallocBase = nullptr;  // device address of the no-alloc staging array, fetched by this context's first no-alloc call
 };
 
 namespace blz {

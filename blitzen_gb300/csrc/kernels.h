@@ -214,6 +214,8 @@ cudaError_t launch_transforms_scatter(BlzMeshTransform* table, uint32_t tableCou
 cudaError_t launch_transforms_rotate(const BlzMeshTransform* table, uint32_t tableCount, const BlzMeshTransform* dynRows,
                                      uint32_t dynCount, const uint32_t* ids, const float* axes, float angle, uint32_t n,
                                      BlzMeshTransform* dst, unsigned int* status, cudaStream_t s);
+// *out = atomicExch(status, 0) on the stream (one thread).
+cudaError_t launch_take_status(unsigned int* status, unsigned int* out, cudaStream_t s);
 cudaError_t launch_depth_raster(const BlzCameraViewData& view, const float* boxes, uint32_t boxCount, float* depth,
                                 uint32_t width, uint32_t height, cudaStream_t s, uint32_t* launches);
 

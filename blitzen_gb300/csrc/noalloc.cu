@@ -8,9 +8,13 @@
 // same two kernels with that staging in `g_noallocScratch` below, a file-scope array sized for at
 // most BLZ_NOALLOC_MAX_OBJECTS render objects, and rejects larger lists instead of growing.
 //
-// Set-up: the array's device address is fetched with cudaGetSymbolAddress once per device, by
-// the first call made with that device current. Make that first call before any stream capture.
-// After set-up a call only validates its arguments and launches.
+// Set-up: the array's device address is fetched with cudaGetSymbolAddress by the first call made on
+// each context (with the context's device current) and kept in the context. Make that first call
+// before any stream capture: a first call inside a capture is refused with an error, since the
+// address lookup can load this file's device code, which a capture cannot record. After set-up a
+// call only validates its arguments and launches. Keeping the address per context, not per
+// device for the process, means a context created after cudaDeviceReset fetches the address of
+// the reloaded module instead of reusing a dead one.
 //
 // Nothing in the array has to start at zero: each call writes every word it later reads (each
 // chunk's count and staged records are written by the decide kernel before the scatter kernel
@@ -39,21 +43,22 @@ static_assert(kCountsOffset % 256 == 0, "regions start on 256-byte lines");
 
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
 
-constexpr int kMaxDevices = 64;
 std::mutex g_setupLock;
-unsigned char* g_base[kMaxDevices] = {};  // device address of g_noallocScratch, per device
 
-// Fetches the array's address for `device` (which is current) on its first use.
-int scratch_base(int device, unsigned char** out) {
+// The array's device address for context c (whose device is current), fetched on first use.
+int scratch_base(blz_ctx* c, unsigned char** out) {
     std::lock_guard<std::mutex> guard(g_setupLock);
-    if (!g_base[device]) {
+    if (!c->noallocBase) {
+        if (c->capturing)
+            return fail(BLZ_ERR_INVALID_ARGUMENT,
+                        "blz_cull_frustum_noalloc's first call on a context must come before any capture: it looks up its staging array");
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress of the no-alloc scratch");
         if (reinterpret_cast<uintptr_t>(p) % 256 != 0) return fail(BLZ_ERR_CUDA, "no-alloc scratch is not 256-byte aligned");
-        g_base[device] = static_cast<unsigned char*>(p);
+        c->noallocBase = static_cast<unsigned char*>(p);
     }
-    *out = g_base[device];
+    *out = c->noallocBase;
     return BLZ_OK;
 }
 
@@ -75,9 +80,8 @@ extern "C" int blz_cull_frustum_noalloc(blz_ctx* c, const BlzCameraViewData* vie
     cudaError_t e = cudaGetDevice(&device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     if (device != c->device) return fail(BLZ_ERR_INVALID_ARGUMENT, "device %d is current, the context is on device %d", device, c->device);
-    if (device < 0 || device >= kMaxDevices) return fail(BLZ_ERR_INVALID_ARGUMENT, "device %d out of range", device);
     unsigned char* base = nullptr;
-    rc = scratch_base(device, &base);
+    rc = scratch_base(c, &base);
     if (rc != BLZ_OK) return rc;
 
     uint32_t chunks = (count + kNoAllocChunk - 1) / kNoAllocChunk;

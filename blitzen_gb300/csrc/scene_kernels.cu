@@ -151,3 +151,14 @@ cudaError_t launch_depth_raster(const BlzCameraViewData& view, const float* boxe
 }
 
 }  // namespace blz
+
+namespace blz {
+
+__global__ void take_status_kernel(unsigned int* status, unsigned int* out) { *out = atomicExch(status, 0u); }
+
+cudaError_t launch_take_status(unsigned int* status, unsigned int* out, cudaStream_t s) {
+    take_status_kernel<<<1, 1, 0, s>>>(status, out);
+    return cudaGetLastError();
+}
+
+}  // namespace blz

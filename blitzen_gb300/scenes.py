@@ -152,6 +152,19 @@ def stress_scene(n: int = 4_000_000, seed: int = 0, n_meshes: int = 64, extent: 
     return Scene(objs, tr, surfaces, lods, boxes=boxes, visibility=vis)
 
 
+STRESS_DEPTH = (1920, 1080)  # the stress frame's depth buffer (width, height)
+STRESS_ZFAR = 1e4
+
+
+def stress_view():
+    """The stress frame's camera: the origin looking +Z, 70 degree vertical field of view at
+    1920x1080, zNear 0.1, zFar 1e4, and the D3D12 pyramid extent (half the depth buffer)."""
+    from . import abi
+    w, h = STRESS_DEPTH
+    return abi.view_setup(fov_radians(), float(w), float(h), ZNEAR, STRESS_ZFAR, (0.0, 0.0, 0.0), 0.0, 0.0,
+                          w / 2, h / 2)
+
+
 def cluster_scene(n: int = 50_000, seed: int = 0, n_meshes: int = 32, clusters_per_mesh: int = 200,
                   extent: float = 1000.0) -> Scene:
     rng = np.random.default_rng(seed)

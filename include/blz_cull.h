@@ -219,9 +219,10 @@ int blz_cull_frustum(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList 
  * up front, or they must not wait on the device-wide synchronisation of cudaFree). Its per-call
  * staging is a fixed device array inside this library, for at most BLZ_NOALLOC_MAX_OBJECTS render
  * objects (8 MiB); longer lists return BLZ_ERR_CAPACITY. Results equal blz_cull_frustum's.
- * The first call with a device current fetches that array's address (cudaGetSymbolAddress), so
- * make it before any stream capture. The array is shared by every
- * context on the device: calls that overlap on the device race on it and must be ordered. */
+ * The first call on each context fetches that array's address (cudaGetSymbolAddress) and keeps it
+ * in the context, so make it before any stream capture (a first call inside a capture returns
+ * BLZ_ERR_INVALID_ARGUMENT). The array is shared by every context on the device: calls that
+ * overlap on the device race on it and must be ordered. */
 #define BLZ_NOALLOC_MAX_OBJECTS (1u << 20)
 int blz_cull_frustum_noalloc(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,
                              const BlzCullTarget* target, blz_stream_t stream);

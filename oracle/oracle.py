@@ -89,21 +89,31 @@ class HostPyramid:
         return self.data[off:off + w * h].reshape(h, w)
 
 
-def pyramid_build(depth: np.ndarray, mode: int = 0) -> HostPyramid:
+def pyramid_build(depth: np.ndarray, mode: int = 0, into: HostPyramid | None = None) -> HostPyramid:
+    """Builds the pyramid of `depth` (into a caller's HostPyramid of the same extent and mode, or a new one)."""
     depth = np.ascontiguousarray(depth, dtype=np.float32)
-    p = HostPyramid(depth.shape[1], depth.shape[0], mode)
+    p = into if into is not None else HostPyramid(depth.shape[1], depth.shape[0], mode)
     lib().bo_pyramid_build(C.byref(p.desc), _ptr(depth))
     return p
 
 
 def cull(mode: int, view: CameraViewData, scene, objects: np.ndarray | None = None, vis: np.ndarray | None = None,
-         pyramid: HostPyramid | None = None, stride: int = 24, capacity: int | None = None, threads: int = 1):
-    """Returns (count, records[min(count,capacity), stride/4] uint32, flags). vis (LATE) is updated in place."""
-    d, keep = scene_desc(scene)
+         pyramid: HostPyramid | None = None, stride: int = 24, capacity: int | None = None, threads: int = 1,
+         out: np.ndarray | None = None, desc=None):
+    """Returns (count, records[min(count,capacity), stride/4] uint32, flags). vis (LATE) is updated in place.
+
+    `out` is an optional caller buffer of at least max(capacity, 1) records of stride/4 words, and
+    `desc` an optional (SceneDesc, arrays) pair from scene_desc(scene): with both, the call
+    allocates nothing on the Python side."""
+    d, keep = desc if desc is not None else scene_desc(scene)
     objs = keep[0] if objects is None else np.ascontiguousarray(objects)
     n = len(objs)
     cap = n if capacity is None else capacity
-    out = np.zeros((max(cap, 1), stride // 4), np.uint32)
+    if out is None:
+        out = np.zeros((max(cap, 1), stride // 4), np.uint32)
+    elif out.dtype != np.uint32 or out.ndim != 2 or out.shape[1] != stride // 4 or out.shape[0] < max(cap, 1) \
+            or not out.flags.c_contiguous:
+        raise ValueError("out must be C-contiguous uint32 [>= capacity, stride/4]")
     flags = C.c_uint32(0)
     cnt = lib().bo_cull(mode, C.byref(view), C.byref(d), _ptr(objs), n, _ptr(vis),
                         C.byref(pyramid.desc) if pyramid else None, _ptr(out), stride, cap, C.byref(flags), threads)

@@ -64,6 +64,27 @@ def test_noalloc_equals_existing_two_calls_in_a_row(scene_ctx):
     assert_records_equal(t.read(), (n, recs), "oracle")
 
 
+# every single-view launch shape blz_ctx_set_launch_shape accepts (threads, objects per thread)
+SHAPES = [(256, 1), (256, 2), (256, 4), (128, 2), (128, 4), (512, 1)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_noalloc_equals_existing_under_every_launch_shape(scene_ctx, shape):
+    """The fixed 512-object chunks of the no-alloc entry point under each launch shape, two calls in
+    a row, against blz_cull_frustum under the same shape."""
+    c, sc = scene_ctx
+    c.set_launch_shape(*shape)
+    try:
+        for k, v in enumerate([view_for(zfar=2500.0, yaw=0.7), view_for(zfar=1e30, position=(-30.0, 10.0, 5.0))]):
+            a, b = Target.alloc(sc.count), Target.alloc(sc.count)
+            assert _noalloc(c, v, a) == 0, abi.load().blz_last_error()
+            assert _existing(c, v, b) == 0, abi.load().blz_last_error()
+            assert c.check() == 0
+            assert_records_equal(a.read(), b.read(), f"shape {shape} call {k}")
+    finally:
+        c.set_launch_shape(256, 2)
+
+
 def test_noalloc_at_the_object_bound_and_after_a_short_list(scene_ctx):
     c, sc = scene_ctx
     reps = -(-abi.NOALLOC_MAX_OBJECTS // sc.count)
