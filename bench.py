@@ -1,22 +1,24 @@
 """Benchmark of the GPU-driven cull path (one JSON line on rank 0).
 
 Workload (the stress configuration): 4,000,000 render objects in [-5000,5000]^3 over 64 meshes x 4
-LODs; one step is one occlusion frame of the reference's D3D12 path (dx12Draw.cpp:590-641):
-  pass 1  blz_cull_first   — objects visible last frame (random 50% bitmask), frustum + LOD
-  pyramid blz_pyramid_build — single-pass Hi-Z over a 1920x1080 fp32 reverse-Z depth buffer
-  pass 2  blz_cull_late    — every object, frustum + Hi-Z + LOD, visibility rewritten
+LODs; one step is one occlusion frame of the reference's path (VulkanRenderer::DrawFrame,
+vulkanDraw.cpp:1015-1031; dx12Draw.cpp:590-641), the draws aside:
+  pass 1   objects visible last frame (random 50% bitmask): frustum + LOD, pass-1 records
+  pyramid  Hi-Z over a 1920x1080 fp32 reverse-Z depth buffer (2,000 occluder boxes)
+  pass 2   every object: frustum + Hi-Z + LOD, pass-2 records, visibility rewritten
 Inputs are resident in HBM when the timed region starts; before each step the visibility buffer is
 restored to the 50% mask and L2 is flushed (a 512 MiB read), both outside the timed events.
 
-value  = objects per second of the device-timed frames: each step replays the frame (the three passes,
-         recorded once with blz_capture_begin/end) as one CUDA graph between two CUDA events; the
-         per-pass breakdown in `roofline` replays each pass as its own graph.
+value  = objects per second of the device-timed frames: each step replays blz_cull_frame (recorded
+         once with blz_capture_begin/end) as one CUDA graph between two CUDA events. The frame's
+         other forms (blz_frame_first + blz_pyramid_build + blz_frame_late; blz_cull_first +
+         blz_pyramid_build + blz_cull_late) are timed the same way in `frame_forms`, and every part
+         as its own graph in `roofline.others`. All three forms give the same records, counts,
+         pyramid and visibility, checked against the oracle (`bit_exact`).
 e2e    = the same frame through the C ABI with host buffers, all inside the timed region: the host
          writes the 1,000 dynamic transform rows into a pinned buffer and replays the recorded step
-         (blz_graph_launch): the 8.3 MB depth upload runs beside the transform update (whose kernel
-         reads the rows from pinned memory) and pass 1, then the pyramid and pass 2, and the
-         scatter kernels write both draw counts into pinned host memory, which the host reads. `with_copies` is the same with an explicit depth upload
-         and count read-back copies; `direct_calls` also calls the three passes directly.
+         (blz_graph_launch): the 8.3 MB depth upload and the pyramid run beside blz_frame_first,
+         then blz_frame_late, and both draw counts land in pinned host memory, which the host reads.
 --impl reference runs the CPU oracle (a port of the reference's shaders, all host threads) on the
 same frames.
 """
@@ -281,13 +283,27 @@ def main():
 
     n_prev = int(sc.visibility.sum())
 
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
     side = torch.cuda.Stream(dev)  # graphs are captured from, and replayed on, a non-default stream
 
-    def step_direct():
+    # The frame in the library's three forms, each one step of the workload:
+    #   one_call        blz_cull_frame: pass 1 over every object (keeping the frustum survivors),
+    #                   the pyramid, the survivors' pyramid test, both record lists in one launch
+    #   kept_frame      blz_frame_first, blz_pyramid_build, blz_frame_late (the renderer's order)
+    #   separate_calls  blz_cull_first, blz_pyramid_build, blz_cull_late (each pass on its own)
+    def frame_one_call():
+        c.cull_frame(v, vis, depth, pyr, t1, t2)
+
+    def frame_kept():
+        c.frame_first_pass(v, vis, t1)
+        c.generate_depth_pyramid(pyr, depth)
+        c.frame_occlusion_pass(pyr, t2)
+
+    def frame_calls():
         c.draw_cull_first_pass(v, vis, t1)
         c.generate_depth_pyramid(pyr, depth)
         c.draw_cull_occlusion_pass(v, vis, pyr, t2)
+
+    forms = {"one_call": frame_one_call, "kept_frame": frame_kept, "separate_calls": frame_calls}
 
     # the oracle's answer for this frame (every host thread), the reference every check below uses
     threads = os.cpu_count() or 1
@@ -296,123 +312,112 @@ def main():
     want = ((o1[0], o1[1].copy()), (o2[0], o2[1].copy()), opyr.data.copy(), ovis.copy())
     exact = {}
 
-    with torch.cuda.stream(side):
-        for _ in range(max(args.warmup, 3)):
+    def timed(g, n):
+        """n replays of graph g, each after restoring the visibility mask and flushing L2 (both outside
+        the events); the per-replay CUDA-event times in ms."""
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for a, b in evs:
             vis.copy_(vis0)
-            step_direct()
+            flush_l2()
+            a.record()
+            g.launch()
+            b.record()
         side.synchronize()
-        c.check()
+        return [a.elapsed_time(b) for a, b in evs]
+
+    with torch.cuda.stream(side):
+        for name, fn in forms.items():
+            for _ in range(max(args.warmup, 3)):
+                vis.copy_(vis0)
+                fn()
+            side.synchronize()
+            c.check()
+            exact[name] = frame_matches(want, t1, t2, vis, pyr)
         V1, _ = t1.read()
         V2, _ = t2.read()
-        exact["direct_calls"] = frame_matches(want, t1, t2, vis, pyr)
-        # the frame as three recorded passes, replayed back to back (no host work between kernels)
-        # the frame (pass 1, pyramid, pass 2) recorded once and replayed as one graph per step; the
-        # three passes are also recorded one by one for the per-pass breakdown
-        c.capture_begin()
-        step_direct()
-        frame = c.capture_end()
-        kernels_per_step = frame.kernels
-        passes = []
-        for fn in (lambda: c.draw_cull_first_pass(v, vis, t1), lambda: c.generate_depth_pyramid(pyr, depth),
-                   lambda: c.draw_cull_occlusion_pass(v, vis, pyr, t2)):
+        graphs = {}
+        for name, fn in forms.items():
             c.capture_begin()
             fn()
-            passes.append(c.capture_end())
-        # the frame without pass 2, for pass 2's time inside the frame (frame minus this)
+            graphs[name] = c.capture_end()
+        kernels_per_step = graphs["one_call"].kernels
+        # each part on its own, for the breakdown (frame_late reuses what the last pass 1 kept)
+        parts = {}
+        for name, fn in (("frame_first", lambda: c.frame_first_pass(v, vis, t1)),
+                         ("pyramid", lambda: c.generate_depth_pyramid(pyr, depth)),
+                         ("frame_late", lambda: c.frame_occlusion_pass(pyr, t2)),
+                         ("pass1", lambda: c.draw_cull_first_pass(v, vis, t1)),
+                         ("pass2", lambda: c.draw_cull_occlusion_pass(v, vis, pyr, t2))):
+            c.capture_begin()
+            fn()
+            parts[name] = c.capture_end()
+        # the separate-calls frame without pass 2 (pass 2 inside that frame = the difference)
         c.capture_begin()
         c.draw_cull_first_pass(v, vis, t1)
         c.generate_depth_pyramid(pyr, depth)
         frame_ab = c.capture_end()
-
-        def step(e=None):
-            if e:
-                e[0].record()
-            frame.launch()
-            if e:
-                e[1].record()
-
-        def step_passes(e):
-            for j, g in enumerate(passes):
-                e[j].record()
-                g.launch()
-            e[3].record()
-
-        for _ in range(max(args.warmup, 3)):
-            vis.copy_(vis0)
-            step()
-        side.synchronize()
+        head = graphs["one_call"]
+        timed(head, max(args.warmup, 3))
 
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
         with ClockSampler(local) as clocks:
             wall0 = time.perf_counter()
-            for k in range(args.steps):
-                vis.copy_(vis0)
-                flush_l2()
-                step(ev[k])
-            side.synchronize()
+            ms = timed(head, args.steps)
             wall = time.perf_counter() - wall0
             launches = kernels_per_step * args.steps
             # keep the same load on the GPU until the sampler has seen at least 1.5 s of it
             while not args.no_clock_hold and time.perf_counter() - wall0 < 1.5:
-                for _ in range(20):
-                    vis.copy_(vis0)
-                    flush_l2()
-                    step()
-                side.synchronize()
+                timed(head, 20)
         # the state the last timed replay left: both record lists, the pyramid and the visibility
         exact["timed_frame"] = frame_matches(want, t1, t2, vis, pyr)
-        # per-pass breakdown (not part of the headline): each pass replayed as its own graph, and the
-        # frame without pass 2 (pass 2 inside the frame = frame - that, launch overheads cancelling)
-        evp = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
-        evab = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
-        for k in range(args.steps):
-            vis.copy_(vis0)
-            flush_l2()
-            step_passes(evp[k])
-            vis.copy_(vis0)
-            flush_l2()
-            evab[k][0].record()
-            frame_ab.launch()
-            evab[k][1].record()
-        side.synchronize()
+        t_form = {name: statistics.mean(timed(g, args.steps)) for name, g in graphs.items()}
+        t_part = {name: statistics.mean(timed(g, args.steps)) for name, g in parts.items()}
+        t_ab = statistics.mean(timed(frame_ab, args.steps))
     c.check()
-    ms = [(e[0].elapsed_time(e[1])) for e in ev]
-    ms_first = [e[0].elapsed_time(e[1]) for e in evp]
-    ms_pyr = [e[1].elapsed_time(e[2]) for e in evp]
-    ms_late_own = [e[2].elapsed_time(e[3]) for e in evp]
-    ms_ab = [e[0].elapsed_time(e[1]) for e in evab]
     t_step = max_over_ranks(sum(ms) / len(ms), world, dev)
     if world > 1:
         dist.barrier()
     value = job_throughput(N, world, t_step)
 
-    # roofline of the dominant kernel (pass 2) and the others, algorithmic bytes
+    # roofline: the dominant kernel of the frame is the kept frame's pass 1 (every object's render
+    # object, transform and visibility read once); algorithmic bytes per launch are the bytes the
+    # reference's passes must move for it: render object + transform + visibility word per object,
+    # the visibility words it settles (candidates outside the frustum) and pass 1's records
     stride = abi.STRIDE_VULKAN
     mip_bytes = pyr.storage.numel() * 4
+    bytes_pyr = W * H * 4 + mip_bytes
+    bytes_a = N * (8 + 32 + 4) + 4 * (n_prev - V1) + V1 * stride + 4
+    bytes_frame = N * (8 + 32) + 4 * N + 4 * N + (V1 + V2) * stride + 8 + bytes_pyr
     bytes_late = N * (8 + 32) + 4 * N + 4 * N + V2 * stride + 4
     bytes_first = 4 * N + n_prev * (8 + 32) + V1 * stride + 4
-    bytes_pyr = W * H * 4 + mip_bytes
     peak, peak_kind = peaks()
-    t_late_own = sum(ms_late_own) / len(ms_late_own)
-    t_late = sum(ms) / len(ms) - sum(ms_ab) / len(ms_ab)  # pass 2 inside the frame
-    t_first = sum(ms_first) / len(ms_first)
-    t_pyr = sum(ms_pyr) / len(ms_pyr)
-    ach = bytes_late / (t_late * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "pass 2: cull_decide_kernel<LATE> + cull_scatter_kernel", "achieved": ach, "peak": peak,
-                "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind, "traffic": None,
-                "algorithmic_bytes": bytes_late, "ms": t_late,
-                "ms_note": "pass 2 inside the recorded frame: frame time minus the time of the frame without pass 2",
-                "standalone_ms": t_late_own, "standalone_frac": bytes_late / (t_late_own * 1e-3) / 1e9 / peak,
+    t_a = t_part["frame_first"]
+    ach = bytes_a / (t_a * 1e-3) / 1e9
+
+    def gbs(b, t):
+        return b / (t * 1e-3) / 1e9
+
+    roofline = {"bound": "hbm", "kernel": "kept-frame pass 1: cull_decide_kernel<4> + cull_scatter_kernel",
+                "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
+                "traffic": None, "algorithmic_bytes": bytes_a, "ms": t_a,
+                "ms_note": "the kept frame's pass 1 (blz_frame_first) recorded as its own graph",
                 "others": {
-                    "pass1": {"ms": t_first, "bytes": bytes_first, "GB/s": bytes_first / (t_first * 1e-3) / 1e9},
-                    "pyramid": {"ms": t_pyr, "bytes": bytes_pyr, "GB/s": bytes_pyr / (t_pyr * 1e-3) / 1e9},
-                    "frame": {"ms": t_step, "bytes": bytes_first + bytes_pyr + bytes_late,
-                              "GB/s": (bytes_first + bytes_pyr + bytes_late) / (t_step * 1e-3) / 1e9}}}
-    # DRAM bytes of one pass-2 decide launch from an ncu capture (profiles/dram_traffic.json names the
-    # commit and the command it was taken with); a capture, not a measurement of this run
-    traffic = recorded_traffic("cull_decide_kernel<LATE>", args.objects)
+                    "frame": {"ms": t_step, "bytes": bytes_frame, "GB/s": gbs(bytes_frame, t_step),
+                              "frac": gbs(bytes_frame, t_step) / peak,
+                              "note": "blz_cull_frame; bytes: every object's tables and visibility read once, "
+                                      "visibility written once, both record lists, the pyramid"},
+                    "frame_late": {"ms": t_part["frame_late"], "note": "survivors' pyramid test + scatter"},
+                    "pyramid": {"ms": t_part["pyramid"], "bytes": bytes_pyr, "GB/s": gbs(bytes_pyr, t_part["pyramid"])},
+                    "pass1": {"ms": t_part["pass1"], "bytes": bytes_first, "GB/s": gbs(bytes_first, t_part["pass1"])},
+                    "pass2": {"ms": t_part["pass2"], "bytes": bytes_late, "GB/s": gbs(bytes_late, t_part["pass2"]),
+                              "ms_in_separate_frame": t_form["separate_calls"] - t_ab,
+                              "frac_in_separate_frame": gbs(bytes_late, t_form["separate_calls"] - t_ab) / peak}}}
+    frames = {name: {"ms": t, "objects_per_s": job_throughput(N, world, t)} for name, t in t_form.items()}
+    # DRAM bytes per launch from an ncu capture (profiles/dram_traffic.json names the commit and the
+    # command it was taken with); a capture, not a measurement of this run
+    traffic = recorded_traffic("cull_decide_kernel<4>", args.objects)
     if traffic:
         roofline["traffic"] = traffic["bytes_per_launch"]
         roofline["traffic_source"] = traffic["source"]
@@ -445,18 +450,19 @@ def main():
                 out.append(e0.elapsed_time(e1))
         return max_over_ranks(sum(out) / len(out), world, dev)
 
-    # the frame as a user replays it (the recorded frame through blz_graph_launch), and as direct calls
-    t_e2e_copies = e2e_run(frame.launch)
-    t_e2e_direct = e2e_run(step_direct)
+    # the serial forms: update, upload, the recorded one-call frame (or direct calls), count copies
+    t_e2e_copies = e2e_run(graphs["one_call"].launch)
+    t_e2e_direct = e2e_run(frame_one_call)
 
     # The whole step as one recorded graph over fixed pinned host buffers. The host writes the
     # step's 1,000 dynamic transform rows into a pinned buffer bound as the scene's dynamic rows
     # (transforms [0, 1000), the reference's dynamic-object range) and launches the graph. In it:
     #  - the depth upload (a copy-engine node, ~46 us for 8.3 MB over the CPU-GPU link) and the
     #    pyramid build run on a second stream beside pass 1, which does not read the depth;
-    #  - both passes read the dynamic rows straight from pinned memory: no update kernel has to
-    #    read them over the link while the depth upload holds it;
+    #  - both passes read the dynamic rows straight from pinned memory;
     #  - the scatter kernels write both draw counts into pinned host memory, which the host reads.
+    # Pass 1 is the kept frame's (blz_frame_first) and pass 2 tests its survivors (blz_frame_late);
+    # the separate-calls form of the same step is timed beside it.
     hcounts0 = torch.zeros(2, dtype=torch.int32, pin_memory=True)
     t1h = Target(t1.commands, hcounts0[0:1], t1.stride, t1.capacity)
     t2h = Target(t2.commands, hcounts0[1:2], t2.stride, t2.capacity)
@@ -466,32 +472,46 @@ def main():
     c.bind_dynamic_transforms(h_tr)
     fork, join = torch.cuda.Event(), torch.cuda.Event()
     side2 = torch.cuda.Stream(dev)
-    with torch.cuda.stream(side):
-        c.capture_begin()
-        fork.record(side)
-        side2.wait_event(fork)
-        with torch.cuda.stream(side2):
-            depth.copy_(hdepth, non_blocking=True)
-            c.generate_depth_pyramid(pyr, depth)
-        join.record(side2)
-        c.draw_cull_first_pass(v, vis, t1h)
-        side.wait_event(join)
-        c.draw_cull_occlusion_pass(v, vis, pyr, t2h)
-        frame_zc = c.capture_end()
-    zc_ms = []
-    for k in range(args.warmup + args.steps):
-        vis.copy_(vis0)
-        flush_l2()
-        dyn_tr["orientation"] = S.random_unit_quaternions(rng, DYNAMIC)
-        torch.cuda.synchronize()
-        e0.record()
-        h_tr_np[:] = dyn_tr  # the step's input rows, host side
-        frame_zc.launch()
-        e1.record()
-        e1.synchronize()
-        counts = hcounts0.numpy().copy()  # the step's result, already in host memory
-        if k >= args.warmup:
-            zc_ms.append(e0.elapsed_time(e1))
+
+    def record_step(pass1, pass2):
+        with torch.cuda.stream(side):
+            c.capture_begin()
+            fork.record(side)
+            side2.wait_event(fork)
+            with torch.cuda.stream(side2):
+                depth.copy_(hdepth, non_blocking=True)
+                c.generate_depth_pyramid(pyr, depth)
+            join.record(side2)
+            pass1()
+            side.wait_event(join)
+            pass2()
+            return c.capture_end()
+
+    step_graphs = {
+        "kept_frame": record_step(lambda: c.frame_first_pass(v, vis, t1h), lambda: c.frame_occlusion_pass(pyr, t2h)),
+        "separate_calls": record_step(lambda: c.draw_cull_first_pass(v, vis, t1h),
+                                      lambda: c.draw_cull_occlusion_pass(v, vis, pyr, t2h)),
+    }
+
+    def zero_copy_run(g):
+        out = []
+        for k in range(args.warmup + args.steps):
+            vis.copy_(vis0)
+            flush_l2()
+            dyn_tr["orientation"] = S.random_unit_quaternions(rng, DYNAMIC)
+            torch.cuda.synchronize()
+            e0.record()
+            h_tr_np[:] = dyn_tr  # the step's input rows, host side
+            g.launch()
+            e1.record()
+            e1.synchronize()
+            counts = hcounts0.numpy().copy()  # the step's result, already in host memory
+            if k >= args.warmup:
+                out.append(e0.elapsed_time(e1))
+        return max_over_ranks(sum(out) / len(out), world, dev), counts
+
+    t_e2e_sep, _ = zero_copy_run(step_graphs["separate_calls"])
+    t_e2e, counts = zero_copy_run(step_graphs["kept_frame"])
     # the last recorded step against the oracle on the scene as that step saw it (its dynamic rows)
     edited = S.Scene(sc.objects, sc.transforms.copy(), sc.surfaces, sc.lods, visibility=sc.visibility)
     edited.transforms[:DYNAMIC] = h_tr_np
@@ -500,21 +520,23 @@ def main():
     t2_host = Target(t2.commands, torch.from_numpy(counts[1:2].copy()), t2.stride, t2.capacity)
     exact["e2e_step"] = frame_matches(((e1_[0], e1_[1]), (e2_[0], e2_[1]), eyr.data, evis), t1_host, t2_host, vis, pyr)
     del edited
-    t_e2e = max_over_ranks(sum(zc_ms) / len(zc_ms), world, dev)
-    frame_zc.close()
+    for g in step_graphs.values():
+        g.close()
     c.bind_dynamic_transforms(None)
     c.update_object_transform(dyn_ids, dyn_tr)  # the resident table catches up with the last step's rows
     e2e = {"value": job_throughput(N, world, t_e2e), "unit": "objects/s", "ms_per_step": t_e2e,
            "h2d_bytes_per_step": W * H * 4 + 2 * DYNAMIC * 32, "d2h_bytes_per_step": 8,
            "path": "host writes the 1,000 dynamic transform rows to a pinned buffer bound as the scene's dynamic rows "
                    "(blz_scene_bind_dynamic); one blz_graph_launch of the recorded step: depth upload + pyramid beside "
-                   "pass 1, then pass 2; both passes read the rows over the CPU-GPU link; draw counts written to "
-                   "pinned memory",
+                   "blz_frame_first, then blz_frame_late; both passes read the rows over the CPU-GPU link; draw "
+                   "counts written to pinned memory",
+           "separate_calls": {"value": job_throughput(N, world, t_e2e_sep), "ms_per_step": t_e2e_sep,
+                              "path": "the same step with blz_cull_first / blz_cull_late"},
            "with_copies": {"value": job_throughput(N, world, t_e2e_copies), "ms_per_step": t_e2e_copies,
-                           "path": "blz_transforms_update + depth H2D copy + recorded frame + count D2H copies"},
+                           "path": "blz_transforms_update + depth H2D copy + recorded blz_cull_frame + count D2H "
+                                   "copies, serial"},
            "direct_calls": {"value": job_throughput(N, world, t_e2e_direct), "ms_per_step": t_e2e_direct,
-                            "path": "with copies, and blz_cull_first / blz_pyramid_build / blz_cull_late called "
-                                    "directly"}}
+                            "path": "with copies, and blz_cull_frame called directly"}}
 
     extras = {}
     if not args.no_extras and rank == 0:
@@ -536,6 +558,7 @@ def main():
             "data": "synthetic (seeded)", "config": workload_config(args), "roofline": roofline,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks.summary(),
             "wall_s_timed": wall, "draws": {"pass1": V1, "pass2": V2}, "launch_shape": c.launch_shape(),
+            "frame_forms": frames,
             "bit_exact": all(exact.values()), "bit_exact_checks": exact,
             "extras": extras,
         }

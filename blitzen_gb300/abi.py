@@ -178,6 +178,10 @@ _PROTOS = {
     "blz_cull_frustum_noalloc": (_I, [_P, C.POINTER(CameraViewData), RenderList, C.POINTER(CullTarget), _P]),
     "blz_cull_first": (_I, [_P, C.POINTER(CameraViewData), RenderList, _P, C.POINTER(CullTarget), _P]),
     "blz_cull_late": (_I, [_P, C.POINTER(CameraViewData), RenderList, _P, C.POINTER(Pyramid), C.POINTER(CullTarget), _P]),
+    "blz_frame_first": (_I, [_P, C.POINTER(CameraViewData), RenderList, _P, C.POINTER(CullTarget), _P]),
+    "blz_frame_late": (_I, [_P, C.POINTER(Pyramid), C.POINTER(CullTarget), _P]),
+    "blz_cull_frame": (_I, [_P, C.POINTER(CameraViewData), RenderList, _P, _P, C.POINTER(Pyramid), C.POINTER(CullTarget),
+                            C.POINTER(CullTarget), _P]),
     "blz_cull_temporal": (_I, [_P, C.POINTER(CameraViewData), RenderList, C.POINTER(Pyramid), C.POINTER(CullTarget), _P]),
     "blz_cull_instanced": (_I, [_P, C.POINTER(CameraViewData), RenderList, _P, _P, _U32, _U32, C.POINTER(CullTarget), _P]),
     "blz_cull_clusters": (_I, [_P, C.POINTER(CameraViewData), RenderList, C.POINTER(Pyramid), C.POINTER(CullTarget), _P, _P]),

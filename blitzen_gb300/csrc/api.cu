@@ -229,6 +229,7 @@ int blz_ctx_destroy(blz_ctx* c) {
     if (c->chunkMem) cudaFree(c->chunkMem);
     if (c->instScratch) cudaFree(c->instScratch);
     if (c->clusterMem) cudaFree(c->clusterMem);
+    if (c->frameMem) cudaFree(c->frameMem);
     delete c;
     return BLZ_OK;
 }
@@ -474,6 +475,10 @@ int blz_pyramid_build(blz_ctx* c, const BlzPyramid* p, const float* depth, blz_s
     bp.mipCount = p->mipCount;
     bp.mode = p->mode;
     for (uint32_t i = 0; i < BLZ_PYRAMID_MAX_MIPS; ++i) bp.mipOffset[i] = p->mipOffset[i];
+    bp.done = &c->scratch->pyrDone;
+    bp.vec4 = (p->mode == BLZ_HIZ_D3D12 && p->depthWidth % 4 == 0 && p->depthHeight >= 2 &&
+               p->width == p->depthWidth / 2 && p->height <= p->depthHeight / 2 && p->mipOffset[0] == 0 &&
+               reinterpret_cast<uintptr_t>(depth) % 16 == 0 && reinterpret_cast<uintptr_t>(p->data) % 8 == 0) ? 1u : 0u;
     uint32_t launches = 0;
     cudaError_t e = launch_pyramid_build(bp, reinterpret_cast<cudaStream_t>(stream), &launches);
     if (e != cudaSuccess) return cuda_fail(e, "pyramid launch");
@@ -558,6 +563,192 @@ int blz_cull_late(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list,
 int blz_cull_temporal(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, const BlzPyramid* pyr,
                       const BlzCullTarget* target, blz_stream_t s) {
     return object_cull(c, BLZ_MODE_TEMPORAL, view, list, nullptr, pyr, target, s);
+}
+
+// ------------------------------------------------------------------ kept frames
+
+}  // extern "C"
+
+namespace blz {
+
+// Kept-frame memory for `chunks` chunks of `chunkSize` objects: staged records of pass 1 and of
+// pass 2 (8 bytes per object each), the chunk counts of both passes and of the kept survivors, and
+// the survivors themselves (32 bytes per object). Grown on demand; never inside a capture.
+struct FrameBuffers {
+    uint2 *staged1, *staged2;
+    uint32_t *count1, *count2, *keepCount;
+    void* keep;
+};
+
+static int ensure_frame_scratch(blz_ctx* c, size_t chunks, size_t chunkSize, FrameBuffers& fb) {
+    const size_t objects = chunks * chunkSize;
+    if (objects > c->frameObjects || chunks > c->frameChunks) {
+        if (c->capturing) return fail(BLZ_ERR_CAPACITY, "scratch must grow, which a capture cannot record: run the call once before capturing");
+        if (c->frameMem) {
+            cudaDeviceSynchronize();
+            cudaFree(c->frameMem);
+            c->frameMem = nullptr;
+            c->frameObjects = c->frameChunks = 0;
+        }
+        const size_t wantObj = objects + objects / 8 + 1024, wantChunks = chunks + chunks / 8 + 64;
+        const size_t bytes = wantObj * (2 * sizeof(uint2) + 32) + wantChunks * 3 * sizeof(uint32_t) + 1024;
+        if (cudaMalloc(&c->frameMem, bytes) != cudaSuccess) return fail(BLZ_ERR_OUT_OF_MEMORY, "kept-frame scratch of %zu bytes", bytes);
+        c->frameObjects = wantObj;
+        c->frameChunks = wantChunks;
+        c->frameOpen = false;
+    }
+    char* m = static_cast<char*>(c->frameMem);
+    fb.keep = m;  // 32-byte survivors first: 256-byte aligned
+    m += c->frameObjects * 32;
+    fb.staged1 = reinterpret_cast<uint2*>(m);
+    m += c->frameObjects * sizeof(uint2);
+    fb.staged2 = reinterpret_cast<uint2*>(m);
+    m += c->frameObjects * sizeof(uint2);
+    fb.count1 = reinterpret_cast<uint32_t*>(m);
+    fb.count2 = fb.count1 + c->frameChunks;
+    fb.keepCount = fb.count2 + c->frameChunks;
+    return BLZ_OK;
+}
+
+static PipeParams frame_params(blz_ctx* c, const FrameBuffers& fb, const BlzCameraViewData& view, const BlzRenderObject* objs,
+                               uint32_t count, uint32_t* vis, uint32_t chunkSize, uint32_t tiles) {
+    PipeParams p{};
+    p.sc = c->scene;
+    p.single.view = view;
+    p.single.objects = objs;
+    p.single.count = count;
+    p.single.vis = vis;
+    p.viewCount = 1;
+    p.totalTiles = tiles;
+    p.chunkSize = chunkSize;
+    p.scratch = c->scratch;
+    p.workCounter = nullptr;
+    p.keep = fb.keep;
+    p.keepCount = fb.keepCount;
+    return p;
+}
+
+static void set_target(PipeParams& p, const BlzCullTarget* t) {
+    p.single.cmds = static_cast<uint8_t*>(t->commands);
+    p.single.stride = t->stride;
+    p.single.capacity = t->capacity;
+    p.single.drawCount = t->drawCount;
+}
+
+// Validates a frame's pass-1 arguments and binds its memory; nothing is launched.
+static int frame_begin(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, uint32_t* vis,
+                       const BlzCullTarget* target, FrameBuffers& fb, PipeParams& p1, int mode = kModeFrame1) {
+    if (!c || !view) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or view is NULL");
+    int rc = check_target(target);
+    if (rc != BLZ_OK) return rc;
+    const BlzRenderObject* objs = nullptr;
+    uint32_t count = 0;
+    rc = resolve_list(c, list, &objs, &count);
+    if (rc != BLZ_OK) return rc;
+    if (count && !vis) return fail(BLZ_ERR_INVALID_ARGUMENT, "visibility buffer is NULL");
+    const uint32_t tile = single_chunk_size(static_cast<uint32_t>(mode), c->singleThreads, c->singleOpt, count, c->smCount);
+    uint32_t tiles = (count + tile - 1) / tile;
+    if (tiles == 0) tiles = 1;  // an empty list still gets one chunk, and its draw counts are written
+    rc = ensure_frame_scratch(c, tiles, tile, fb);
+    if (rc != BLZ_OK) return rc;
+    p1 = frame_params(c, fb, *view, objs, count, vis, tile, tiles);
+    p1.single.mode = BLZ_MODE_FIRST;
+    p1.staged = fb.staged1;
+    p1.chunkCount = fb.count1;
+    set_target(p1, target);
+    return BLZ_OK;
+}
+
+static void frame_keep(blz_ctx* c, const PipeParams& p1) {
+    c->frameOpen = true;
+    c->frameView = p1.single.view;
+    c->frameObjs = p1.single.objects;
+    c->frameCount = p1.single.count;
+    c->frameVis = p1.single.vis;
+    c->frameChunkSize = p1.chunkSize;
+    c->frameTiles = p1.totalTiles;
+}
+
+// Pass-2 parameters of the context's open frame.
+static int frame_late_params(blz_ctx* c, const BlzPyramid* pyr, const BlzCullTarget* target, PipeParams& p2) {
+    int rc = check_target(target);
+    if (rc != BLZ_OK) return rc;
+    rc = check_pyramid(pyr, true);
+    if (rc != BLZ_OK) return rc;
+    FrameBuffers fb{};
+    rc = ensure_frame_scratch(c, c->frameTiles, c->frameChunkSize, fb);  // binds only: the frame's chunks fit
+    if (rc != BLZ_OK) return rc;
+    p2 = frame_params(c, fb, c->frameView, c->frameObjs, c->frameCount, c->frameVis, c->frameChunkSize, c->frameTiles);
+    p2.single.mode = BLZ_MODE_LATE;
+    p2.single.pyr = pyramid_view(pyr);
+    p2.staged = fb.staged2;
+    p2.chunkCount = fb.count2;
+    set_target(p2, target);
+    return BLZ_OK;
+}
+
+}  // namespace blz
+
+extern "C" {
+
+int blz_frame_first(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, uint32_t* vis,
+                    const BlzCullTarget* target, blz_stream_t stream) {
+    FrameBuffers fb{};
+    PipeParams p1{};
+    int rc = frame_begin(c, view, list, vis, target, fb, p1);
+    if (rc != BLZ_OK) return rc;
+    cudaError_t e = launch_frame_first(p1, c->singleThreads, c->singleOpt, c->smCount, reinterpret_cast<cudaStream_t>(stream), true);
+    if (e != cudaSuccess) return cuda_fail(e, "frame pass-1 launch");
+    c->launches += 2;  // decide + scatter
+    frame_keep(c, p1);
+    return BLZ_OK;
+}
+
+int blz_frame_late(blz_ctx* c, const BlzPyramid* pyr, const BlzCullTarget* target, blz_stream_t stream) {
+    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (!c->frameOpen) return fail(BLZ_ERR_INVALID_ARGUMENT, "blz_frame_late needs a blz_frame_first on this context first");
+    PipeParams p2{};
+    int rc = frame_late_params(c, pyr, target, p2);
+    if (rc != BLZ_OK) return rc;
+    cudaError_t e = launch_frame_late(p2, c->smCount, reinterpret_cast<cudaStream_t>(stream), true);
+    if (e != cudaSuccess) return cuda_fail(e, "frame pass-2 launch");
+    c->launches += 2;  // survivors' pyramid test + scatter
+    return BLZ_OK;
+}
+
+int blz_cull_frame(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, uint32_t* vis, const float* depth,
+                   const BlzPyramid* pyr, const BlzCullTarget* target1, const BlzCullTarget* target2, blz_stream_t stream) {
+    FrameBuffers fb{};
+    PipeParams p1{};
+    int rc = frame_begin(c, view, list, vis, target1, fb, p1, kModeFrameFused);
+    if (rc != BLZ_OK) return rc;
+    rc = check_target(target2);
+    if (rc != BLZ_OK) return rc;
+    rc = check_pyramid(pyr, true);
+    if (rc != BLZ_OK) return rc;
+    if (!depth) return fail(BLZ_ERR_INVALID_ARGUMENT, "depth is NULL");
+    if (pyr->depthWidth == 0 || pyr->depthHeight == 0) return fail(BLZ_ERR_INVALID_ARGUMENT, "pyramid has no depth extent");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    // the pyramid, then one sweep deciding both passes, then both record lists in one launch
+    rc = blz_pyramid_build(c, pyr, depth, stream);
+    if (rc != BLZ_OK) return rc;
+    PipeParams p2 = p1;  // pass 2's records: staged / chunkCount, target 2
+    p2.single.mode = BLZ_MODE_LATE;
+    p2.single.pyr = pyramid_view(pyr);
+    p2.staged = fb.staged1;
+    p2.chunkCount = fb.count1;
+    set_target(p2, target2);
+    p2.staged2 = fb.staged2;  // pass 1's records
+    p2.chunkCount2 = fb.count2;
+    cudaError_t e = launch_frame_fused(p2, c->singleThreads, c->singleOpt, c->smCount, st);
+    PipeParams q1 = p1;  // pass 1's list for the scatter
+    q1.staged = fb.staged2;
+    q1.chunkCount = fb.count2;
+    if (e == cudaSuccess) e = launch_frame_scatter2(q1, p2, st);
+    if (e != cudaSuccess) return cuda_fail(e, "frame launch");
+    c->launches += 2;  // the sweep + both scatters
+    c->frameOpen = false;  // the fused sweep keeps no survivors for blz_frame_late
+    return BLZ_OK;
 }
 
 int blz_cull_instanced(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, BlzLodInstanceCounter* counters,

@@ -48,6 +48,15 @@ struct blz_ctx {
     BlzLaunchShape shape{256, 2, 0, 0};   // batch launches
     uint32_t singleThreads = 256, singleOpt = 2;  // single-view launches
     unsigned char* noallocBase = nullptr;  // device address of the no-alloc staging array, fetched by this context's first no-alloc call
+    // kept frame (blz_frame_first / blz_frame_late): staged records of both passes, their chunk
+    // counts, the survivors pass 1 keeps and their counts, and what pass 2 reuses of pass 1's call
+    void* frameMem = nullptr;
+    size_t frameObjects = 0, frameChunks = 0;
+    bool frameOpen = false;
+    BlzCameraViewData frameView{};
+    const BlzRenderObject* frameObjs = nullptr;
+    uint32_t frameCount = 0, frameChunkSize = 0, frameTiles = 0;
+    uint32_t* frameVis = nullptr;
 };
 
 namespace blz {

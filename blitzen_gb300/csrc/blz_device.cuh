@@ -285,7 +285,7 @@ struct Scratch {
     unsigned int ticket;
     unsigned int epoch;
     unsigned int doneBlocks;
-    unsigned int pad0;
+    unsigned int pyrDone;        // pyramid build: tiles finished (zero between builds)
     unsigned int status;         // BLZ_FLAG_* bits
     unsigned int pad1[27];       // keep the state array on its own 128-byte lines
     unsigned long long state[1]; // [maxTiles] tile states: epoch << 32 | flag << 30 | value

@@ -76,39 +76,40 @@ struct Survivor {
 };
 constexpr uint32_t kRing = 64;  // per-warp survivor ring: under 32 waiting plus one 32-object slice
 
-// Dense stage over n <= 32 queued survivors starting at ring index head, in object order: the sphere
+// Dense stage over one survivor per lane (lanes with `mine`), in object order: the sphere
 // projection and Hi-Z test (LATE/TEMPORAL), LATE's visibility write, LOD selection of the emitted
 // ones, and their staging as (objectId, lodId) after the `run` already staged for the chunk.
+// A survivor is the two words of a Survivor: a = {obj | tags, centre}, b = {r, scale, lodOff, lodCnt}.
+// kModeFrame1 emits the survivors visible last frame (its pass-1 records) and tests no pyramid.
+// kModeFrameFused stages pass 2's records in `stage` and pass 1's in `stage1` (run1).
 template <int MODE>
-__device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchViewDev& bv, const ViewConsts& v,
-                                            const Survivor* ring, uint32_t head, uint32_t n, uint2* stage,
-                                            uint32_t& run) {
-    const uint32_t lane = threadIdx.x & 31u;
-    const bool mine = lane < n;
-    uint4 a = make_uint4(0u, 0u, 0u, 0u), b = make_uint4(0u, 0u, 0u, 0u);
-    if (mine) {
-        const uint4* e = reinterpret_cast<const uint4*>(ring + ((head + lane) & (kRing - 1u)));
-        a = e[0];
-        b = e[1];
-    }
+__device__ __forceinline__ void dense_entry(const SceneTables& sc, const BatchViewDev& bv, const ViewConsts& v, uint4 a,
+                                            uint4 b, bool mine, uint2* stage, uint32_t& run, uint2* stage1 = nullptr,
+                                            uint32_t* run1 = nullptr) {
+    constexpr bool FUSED = MODE == kModeFrameFused;
+    constexpr bool REWRITE = MODE == BLZ_MODE_LATE || FUSED;  // pass 2's visibility rewrite
     const uint32_t obj = a.x & 0x3FFFFFFFu;  // LATE: bit 31 previous visibility != 0, bit 30 == 1
     const Vec3 c{__uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(a.w)};
     const float r = __uint_as_float(b.x), scale = __uint_as_float(b.y);
+    const bool wasNonZero = (a.x >> 31) != 0u;
     bool visible = mine;
     if (mine) {
-        if (MODE == BLZ_MODE_LATE || MODE == BLZ_MODE_TEMPORAL) {
+        if (MODE == BLZ_MODE_LATE || MODE == BLZ_MODE_TEMPORAL || FUSED) {
             float4 aabb;
             if (project_sphere(c, r, v.zNear, v.proj0, v.proj5, aabb)) visible = occlusion(aabb, bv.pyr, v, c, r);
         }
-        if (MODE == BLZ_MODE_LATE) {
+        if (REWRITE) {
             // drawOccLate.cs.hlsl:67, storing only a value that changes
-            const bool wasNonZero = (a.x >> 31) != 0u, wasOne = ((a.x >> 30) & 1u) != 0u;
+            const bool wasOne = ((a.x >> 30) & 1u) != 0u;
             if (visible ? !wasOne : wasNonZero) bv.vis[obj] = visible ? 1u : 0u;
         }
     }
-    const bool emitted = visible && (MODE == BLZ_MODE_LATE ? (a.x >> 31) == 0u : true);  // drawOccLate.cs.hlsl:45
+    // drawOccLate.cs.hlsl:45; a kept frame's pass 1 emits what drawOccFirst.cs.hlsl:22-25 admits
+    const bool emitted = visible && (REWRITE ? !wasNonZero : (MODE == kModeFrame1 ? wasNonZero : true));
+    // the fused sweep's pass 1: every survivor visible last frame (its frustum test passed)
+    const bool emitted1 = FUSED && mine && wasNonZero;
     uint32_t lid = 0u;
-    if (emitted) {
+    if (emitted || emitted1) {
         // cullBuffers.hlsl:42-55 — last LOD in [1, lodCount) with error < threshold
         const float threshold = lod_threshold(c, r, scale, v.lodTarget);
         uint32_t sel = 0;
@@ -119,6 +120,33 @@ __device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchVi
     const unsigned e = __ballot_sync(0xFFFFFFFFu, emitted);
     if (emitted) stage[run + __popc(e & lanemask_lt())] = make_uint2(obj, lid);
     run += __popc(e);
+    if constexpr (FUSED) {
+        const unsigned e1 = __ballot_sync(0xFFFFFFFFu, emitted1);
+        if (emitted1) stage1[*run1 + __popc(e1 & lanemask_lt())] = make_uint2(obj, lid);
+        *run1 += __popc(e1);
+    }
+}
+
+// dense_entry over n <= 32 queued survivors starting at ring index head. kModeFrame1 also appends
+// them to the chunk's kept survivors (keep[kept ...], 32 bytes each, coalesced).
+template <int MODE>
+__device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchViewDev& bv, const ViewConsts& v,
+                                            const Survivor* ring, uint32_t head, uint32_t n, uint2* stage,
+                                            uint32_t& run, uint4* keep, uint32_t& kept, uint2* stage1, uint32_t* run1) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool mine = lane < n;
+    uint4 a = make_uint4(0u, 0u, 0u, 0u), b = make_uint4(0u, 0u, 0u, 0u);
+    if (mine) {
+        const uint4* e = reinterpret_cast<const uint4*>(ring + ((head + lane) & (kRing - 1u)));
+        a = e[0];
+        b = e[1];
+        if constexpr (MODE == kModeFrame1) {
+            keep[2u * (kept + lane)] = a;
+            keep[2u * (kept + lane) + 1u] = b;
+        }
+    }
+    if constexpr (MODE == kModeFrame1) kept += n;
+    dense_entry<MODE>(sc, bv, v, a, b, mine, stage, run, stage1, run1);
 }
 
 // The fields of the surface table the frustum stage reads (bounding sphere; LOD offset and count),
@@ -144,7 +172,8 @@ struct SurfaceCache {
 template <int MODE, bool SINGLE, int OPT>
 __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const BatchViewDev& bv, uint32_t base,
                                                     uint32_t limit, uint2* stage, Survivor* ring, uint4* cand,
-                                                    const SurfaceCache& surf, unsigned int& flags) {
+                                                    const SurfaceCache& surf, unsigned int& flags, uint4* keep,
+                                                    uint32_t& kept, uint2* stage1 = nullptr, uint32_t* run1 = nullptr) {
     constexpr uint32_t STEP = 32u * OPT;
     constexpr bool PACK = (MODE == BLZ_MODE_FIRST) && SINGLE;  // candidate ring of 2 * STEP entries
     // Single-view pass 2 walks its chunk from the last object down: pass 1 walked the same chunk
@@ -161,7 +190,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
         for (uint32_t i = base + lane; i < limit; i += 32u) {
             const bool act = MODE != BLZ_MODE_FIRST || __ldg(bv.vis + i) != 0u;
             if (act) flags |= BLZ_FLAG_BAD_INDEX;
-            if (MODE == BLZ_MODE_LATE) bv.vis[i] = 0u;
+            if (MODE == BLZ_MODE_LATE || MODE == kModeFrame1 || MODE == kModeFrameFused) bv.vis[i] = 0u;
         }
         return 0u;
     }
@@ -174,7 +203,10 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
     float4 ps[OPT], q[OPT], sph[OPT];
     uint2 lod[OPT];
     bool ok[OPT];
-    auto active = [&](uint32_t obj, uint32_t vis) -> bool { return MODE == BLZ_MODE_LATE ? obj < limit : vis != 0u; };
+    // LATE and kModeFrame1 test every object (vis[k] holds its visibility word), the others the
+    // objects with vis[k] != 0
+    constexpr bool ALL = MODE == BLZ_MODE_LATE || MODE == kModeFrame1 || MODE == kModeFrameFused;
+    auto active = [&](uint32_t obj, uint32_t vis) -> bool { return ALL ? obj < limit : vis != 0u; };
     auto gather = [&](const uint32_t (&obj)[OPT], const uint2 (&ro)[OPT], const uint32_t (&vis)[OPT]) {
 #pragma unroll
         for (int k = 0; k < OPT; ++k) {
@@ -211,18 +243,18 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
             const float r = BLZ_FM(sph[k].w, ps[k].w);
             const bool inFrustum = good && frustum_check(c, r, v);
             // drawOccLate.cs.hlsl:67, storing only a value that changes
-            if (MODE == BLZ_MODE_LATE && act && !inFrustum && vis[k] != 0u) bv.vis[obj[k]] = 0u;
+            if (ALL && act && !inFrustum && vis[k] != 0u) bv.vis[obj[k]] = 0u;
             const unsigned m = __ballot_sync(0xFFFFFFFFu, inFrustum);
             if (inFrustum) {
                 uint4* e = reinterpret_cast<uint4*>(ring + ((tail + __popc(m & lanemask_lt())) & (kRing - 1u)));
-                const uint32_t tag = MODE != BLZ_MODE_LATE ? 0u : (vis[k] != 0u ? 0x80000000u : 0u) | (vis[k] == 1u ? 0x40000000u : 0u);
+                const uint32_t tag = !ALL ? 0u : (vis[k] != 0u ? 0x80000000u : 0u) | (vis[k] == 1u ? 0x40000000u : 0u);
                 e[0] = make_uint4(obj[k] | tag, __float_as_uint(c.x), __float_as_uint(c.y), __float_as_uint(c.z));
                 e[1] = make_uint4(__float_as_uint(r), __float_as_uint(ps[k].w), lod[k].x, lod[k].y);
             }
             tail += __popc(m);
             if (tail - head >= 32u) {
                 __syncwarp();
-                dense_round<MODE>(sc, bv, v, ring, head, 32u, stage, run);
+                dense_round<MODE>(sc, bv, v, ring, head, 32u, stage, run, keep, kept, stage1, run1);
                 head += 32u;
                 __syncwarp();
             }
@@ -239,7 +271,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
             nro[k] = in ? __ldg(reinterpret_cast<const uint2*>(bv.objects) + i) : make_uint2(0u, 0u);
             nvis[k] = in ? 1u : 0u;
             if (MODE == BLZ_MODE_FIRST && in) nvis[k] = __ldg(bv.vis + i);
-            if (MODE == BLZ_MODE_LATE) nvis[k] = in ? bv.vis[i] : 0u;  // rewritten later by this warp: coherent load
+            if (ALL) nvis[k] = in ? bv.vis[i] : 0u;  // rewritten later by this warp: coherent load
         }
     };
     // candidates packed by pass 1, taken STEP at a time (or the rest, at the end)
@@ -294,7 +326,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
     }
     if (tail != head) {
         __syncwarp();
-        dense_round<MODE>(sc, bv, v, ring, head, tail - head, stage, run);
+        dense_round<MODE>(sc, bv, v, ring, head, tail - head, stage, run, keep, kept, stage1, run1);
         __syncwarp();
     }
     return run;
@@ -368,18 +400,27 @@ __global__ void __launch_bounds__(THREADS, (SINGLE || MODE >= 0) ? 1024 / THREAD
         uint2* stage = p.staged + static_cast<size_t>(chunk) * chunkSize;
         Survivor* ring = s_ring[warp];
         uint4* cand = s_cand[PACK ? warp : 0];
-        uint32_t total = 0;
+        uint32_t total = 0, kept = 0, total1 = 0;
+        uint4* keep = nullptr;
+        if constexpr (MODE == kModeFrame1) keep = static_cast<uint4*>(p.keep) + 2u * static_cast<size_t>(chunk) * chunkSize;
+        uint2* stage1 = nullptr;
+        if constexpr (MODE == kModeFrameFused) stage1 = p.staged2 + static_cast<size_t>(chunk) * chunkSize;
         if (MODE == kModeRuntime) {
             switch (bv.mode) {
-                case BLZ_MODE_FIRST: total = decide_run_warp<BLZ_MODE_FIRST, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags); break;
-                case BLZ_MODE_LATE: total = decide_run_warp<BLZ_MODE_LATE, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags); break;
-                case BLZ_MODE_TEMPORAL: total = decide_run_warp<BLZ_MODE_TEMPORAL, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags); break;
-                default: total = decide_run_warp<BLZ_MODE_FRUSTUM, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags); break;
+                case BLZ_MODE_FIRST: total = decide_run_warp<BLZ_MODE_FIRST, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags, keep, kept); break;
+                case BLZ_MODE_LATE: total = decide_run_warp<BLZ_MODE_LATE, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags, keep, kept); break;
+                case BLZ_MODE_TEMPORAL: total = decide_run_warp<BLZ_MODE_TEMPORAL, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags, keep, kept); break;
+                default: total = decide_run_warp<BLZ_MODE_FRUSTUM, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags, keep, kept); break;
             }
         } else {
-            total = decide_run_warp<(MODE < 0 ? 0 : MODE), SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags);
+            total = decide_run_warp<(MODE < 0 ? 0 : MODE), SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags, keep, kept,
+                                                                       stage1, &total1);
         }
-        if (lane == 0) p.chunkCount[chunk] = total;
+        if (lane == 0) {
+            p.chunkCount[chunk] = total;
+            if constexpr (MODE == kModeFrame1) p.keepCount[chunk] = kept;
+            if constexpr (MODE == kModeFrameFused) p.chunkCount2[chunk] = total1;
+        }
         chunk = next;
     }
     if (flags) atomicOr(&p.scratch->status, flags);
@@ -397,13 +438,13 @@ constexpr int kScatterWarps = 32;  // one warp per chunk
 constexpr uint32_t kScatterChunks = 32;
 
 template <bool SINGLE>
-__global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const PipeParams p) {
+__device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_t block) {
     __shared__ uint32_t s_part[kScatterWarps];
     __shared__ uint32_t s_base[kScatterChunks], s_n[kScatterChunks], s_vi[kScatterChunks];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t chunkSize = p.chunkSize;
-    const uint32_t c0 = blockIdx.x * kScatterChunks;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && p.workCounter != nullptr) *p.workCounter = 0u;
+    const uint32_t c0 = block * kScatterChunks;
+    if (block == 0 && threadIdx.x == 0 && p.workCounter != nullptr) *p.workCounter = 0u;
     if (c0 >= p.totalTiles) return;
     const uint32_t vi0 = SINGLE ? 0u : find_view_warp(p.tileStart, p.viewCount, c0);
     const uint32_t viewStart0 = SINGLE ? 0u : __ldg(p.tileStart + vi0);
@@ -505,6 +546,93 @@ __global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const 
     }
 }
 
+template <bool SINGLE>
+__global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const PipeParams p) {
+    scatter_block<SINGLE>(p, blockIdx.x);
+}
+
+// Both record lists of a kept frame in one launch: blocks [0, blocks1) scatter list 1, the rest list 2.
+__global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter2_kernel(const PipeParams p1, const PipeParams p2,
+                                                                           const uint32_t blocks1) {
+    if (blockIdx.x < blocks1) scatter_block<true>(p1, blockIdx.x);
+    else scatter_block<true>(p2, blockIdx.x - blocks1);
+}
+
+// ------------------------------------------------------------------ kept frame, pass 2
+
+// Pass 2 of a kept frame (blz_frame_late): one warp per chunk runs the dense stage of pass 2 over
+// the survivors pass 1 kept for that chunk, in object order: projectSphere and the Hi-Z test
+// (drawOccLate.cs.hlsl:48-58), the visibility rewrite (:67) and the emission of objects not visible
+// last frame (:45), staged as (objectId, lodId) for the scatter. Every object pass 1 did not keep was
+// outside the frustum and got its visibility in pass 1. A lane takes kLateRounds survivors at once
+// (j, j + 32, ...): their loads, tests and LOD selections are independent, so their latencies
+// overlap; they are staged in order afterwards.
+constexpr uint32_t kLateRounds = 4;
+
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) frame_late_kernel(const PipeParams p) {
+    constexpr int NW = THREADS / 32;
+    constexpr uint32_t R = kLateRounds;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t warpsTotal = gridDim.x * NW;
+    const BatchViewDev& bv = p.single;
+    const ViewConsts v = load_view(bv.view);
+    const uint32_t lt = lanemask_lt();
+    for (uint32_t chunk = blockIdx.x * NW + warp; chunk < p.totalTiles; chunk += warpsTotal) {
+        const uint32_t n = __ldcg(p.keepCount + chunk);
+        const uint4* keep = static_cast<const uint4*>(p.keep) + 2u * static_cast<size_t>(chunk) * p.chunkSize;
+        uint2* stage = p.staged + static_cast<size_t>(chunk) * p.chunkSize;
+        uint32_t run = 0;
+        for (uint32_t j0 = 0; j0 < n; j0 += 32u * R) {
+            uint4 a[R], b[R];
+#pragma unroll
+            for (uint32_t r = 0; r < R; ++r) {
+                const uint32_t j = j0 + r * 32u + lane;
+                a[r] = make_uint4(0u, 0u, 0u, 0u);
+                b[r] = a[r];
+                if (j < n) {
+                    a[r] = __ldcg(keep + 2u * j);
+                    b[r] = __ldcg(keep + 2u * j + 1u);
+                }
+            }
+            bool emit[R];
+            uint32_t lid[R];
+#pragma unroll
+            for (uint32_t r = 0; r < R; ++r) {
+                const bool mine = j0 + r * 32u + lane < n;
+                const uint32_t obj = a[r].x & 0x3FFFFFFFu;
+                const Vec3 c{__uint_as_float(a[r].y), __uint_as_float(a[r].z), __uint_as_float(a[r].w)};
+                const float rad = __uint_as_float(b[r].x);
+                bool visible = mine;
+                if (mine) {
+                    float4 aabb;
+                    if (project_sphere(c, rad, v.zNear, v.proj0, v.proj5, aabb)) visible = occlusion(aabb, bv.pyr, v, c, rad);
+                    // drawOccLate.cs.hlsl:67, storing only a value that changes
+                    const bool wasNonZero = (a[r].x >> 31) != 0u, wasOne = ((a[r].x >> 30) & 1u) != 0u;
+                    if (visible ? !wasOne : wasNonZero) bv.vis[obj] = visible ? 1u : 0u;
+                }
+                emit[r] = visible && (a[r].x >> 31) == 0u;  // drawOccLate.cs.hlsl:45
+                lid[r] = 0u;
+                if (emit[r]) {
+                    // cullBuffers.hlsl:42-55 — last LOD in [1, lodCount) with error < threshold
+                    const float threshold = lod_threshold(c, rad, __uint_as_float(b[r].y), v.lodTarget);
+                    uint32_t sel = 0;
+                    for (uint32_t t = 1; t < b[r].w; ++t)
+                        if (__ldg(&p.sc.lods[b[r].z + t].error) < threshold) sel = t;
+                    lid[r] = b[r].z + sel;
+                }
+            }
+#pragma unroll
+            for (uint32_t r = 0; r < R; ++r) {
+                const unsigned e = __ballot_sync(0xFFFFFFFFu, emit[r]);
+                if (emit[r]) stage[run + __popc(e & lt)] = make_uint2(a[r].x & 0x3FFFFFFFu, lid[r]);
+                run += __popc(e);
+            }
+        }
+        if (lane == 0) p.chunkCount[chunk] = run;
+    }
+}
+
 // ------------------------------------------------------------------ launchers
 
 // Resident blocks per SM of one instantiation (a property of the kernel, asked once).
@@ -546,6 +674,74 @@ static cudaError_t launch_t(const PipeParams& p, uint32_t blocksPerSm, int smCou
 
 uint32_t object_tile_size() { return kChunk; }
 
+template <int THREADS, int OPT>
+static cudaError_t launch_frame_first_t(const PipeParams& p, int smCount, cudaStream_t s, bool scatter) {
+    cudaError_t e = launch_decide_t<kModeFrame1, true, THREADS, OPT>(p, 0, smCount, s);
+    if (e != cudaSuccess || !scatter) return e;
+    const uint32_t sgrid = (p.totalTiles + kScatterChunks - 1) / kScatterChunks;
+    cull_scatter_kernel<true><<<sgrid ? sgrid : 1u, kScatterWarps * 32, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_frame_first(const PipeParams& p, uint32_t threads, uint32_t opt, int smCount, cudaStream_t s,
+                               bool scatter) {
+    PipeParams q = p;
+    q.descending = 0u;
+    if (threads == 256 && opt == 1) return launch_frame_first_t<256, 1>(q, smCount, s, scatter);
+    if (threads == 256 && opt == 4) return launch_frame_first_t<256, 4>(q, smCount, s, scatter);
+    if (threads == 128 && opt == 2) return launch_frame_first_t<128, 2>(q, smCount, s, scatter);
+    if (threads == 128 && opt == 4) return launch_frame_first_t<128, 4>(q, smCount, s, scatter);
+    if (threads == 512 && opt == 1) return launch_frame_first_t<512, 1>(q, smCount, s, scatter);
+    return launch_frame_first_t<kObjThreads, kObjOpt>(q, smCount, s, scatter);
+}
+
+cudaError_t launch_frame_fused(const PipeParams& p, uint32_t threads, uint32_t opt, int smCount, cudaStream_t s) {
+    PipeParams q = p;
+    q.descending = 0u;
+    if (threads == 256 && opt == 1) return launch_decide_t<kModeFrameFused, true, 256, 1>(q, 0, smCount, s);
+    if (threads == 256 && opt == 4) return launch_decide_t<kModeFrameFused, true, 256, 4>(q, 0, smCount, s);
+    if (threads == 128 && opt == 2) return launch_decide_t<kModeFrameFused, true, 128, 2>(q, 0, smCount, s);
+    if (threads == 128 && opt == 4) return launch_decide_t<kModeFrameFused, true, 128, 4>(q, 0, smCount, s);
+    if (threads == 512 && opt == 1) return launch_decide_t<kModeFrameFused, true, 512, 1>(q, 0, smCount, s);
+    return launch_decide_t<kModeFrameFused, true, kObjThreads, kObjOpt>(q, 0, smCount, s);
+}
+
+constexpr int kFrameLateThreads = 256;
+
+cudaError_t launch_frame_late(const PipeParams& p, int smCount, cudaStream_t s, bool scatter) {
+    static const uint32_t occ = [] {
+        int o = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, frame_late_kernel<kFrameLateThreads>, kFrameLateThreads, 0) !=
+            cudaSuccess) {
+            (void)cudaGetLastError();
+            o = 1;
+        }
+        return static_cast<uint32_t>(o < 1 ? 1 : o);
+    }();
+    constexpr uint32_t NW = kFrameLateThreads / 32;
+    uint32_t grid = occ * static_cast<uint32_t>(smCount > 0 ? smCount : 1);
+    const uint32_t needed = (p.totalTiles + NW - 1) / NW;
+    if (grid > needed) grid = needed;
+    if (grid == 0) grid = 1;
+    PipeParams q = p;
+    q.descending = 0u;
+    frame_late_kernel<kFrameLateThreads><<<grid, kFrameLateThreads, 0, s>>>(q);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !scatter) return e;
+    const uint32_t sgrid = (q.totalTiles + kScatterChunks - 1) / kScatterChunks;
+    cull_scatter_kernel<true><<<sgrid ? sgrid : 1u, kScatterWarps * 32, 0, s>>>(q);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_frame_scatter2(const PipeParams& p1, const PipeParams& p2, cudaStream_t s) {
+    const uint32_t g1 = (p1.totalTiles + kScatterChunks - 1) / kScatterChunks;
+    const uint32_t g2 = (p2.totalTiles + kScatterChunks - 1) / kScatterChunks;
+    PipeParams q1 = p1, q2 = p2;
+    q1.descending = q2.descending = 0u;
+    cull_scatter2_kernel<<<(g1 ? g1 : 1u) + (g2 ? g2 : 1u), kScatterWarps * 32, 0, s>>>(q1, q2, g1 ? g1 : 1u);
+    return cudaGetLastError();
+}
+
 template <int MODE>
 static uint32_t single_blocks_per_sm(uint32_t threads, uint32_t opt) {
     if (threads == 256 && opt == 1) return occupancy_t<MODE, true, 256, 1>();
@@ -563,6 +759,8 @@ uint32_t single_chunk_size(uint32_t mode, uint32_t threads, uint32_t opt, uint32
     }
     uint32_t per = 1;
     switch (mode) {
+        case kModeFrame1: per = single_blocks_per_sm<kModeFrame1>(threads, opt); break;
+        case kModeFrameFused: per = single_blocks_per_sm<kModeFrameFused>(threads, opt); break;
         case BLZ_MODE_FIRST: per = single_blocks_per_sm<BLZ_MODE_FIRST>(threads, opt); break;
         case BLZ_MODE_LATE: per = single_blocks_per_sm<BLZ_MODE_LATE>(threads, opt); break;
         case BLZ_MODE_TEMPORAL: per = single_blocks_per_sm<BLZ_MODE_TEMPORAL>(threads, opt); break;

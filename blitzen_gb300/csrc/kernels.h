@@ -51,6 +51,18 @@ using SceneT = SceneTablesHost;
 using PyramidT = PyramidViewHost;
 #endif
 
+// Pass 1 of a kept frame (blz_frame_first): every object of the list is frustum-tested once; the
+// objects visible last frame that pass are emitted (pass 1's records), and every object that passes
+// is kept, with its view-space sphere, for the frame's pass 2, which then tests only those against
+// the pyramid (frame_late_kernel). An object outside the frustum gets its final visibility (0) here.
+constexpr int kModeFrame1 = 4;
+// Both passes of a frame in one sweep (blz_cull_frame, the pyramid built first): every object is
+// frustum-tested once, the survivors are tested against the pyramid at once, and each object lands
+// in pass 1's records (visible last frame and inside the frustum), in pass 2's (not visible last
+// frame, inside the frustum and not occluded) or in neither; its visibility is rewritten as pass 2
+// rewrites it. Pass 1's records are staged in staged2 / chunkCount2.
+constexpr int kModeFrameFused = 5;
+
 constexpr int kObjThreads = 256;
 constexpr int kObjOpt = 2;
 constexpr uint32_t kMaxTiles = 1u << 20;             // tile states held by one scratch
@@ -90,6 +102,10 @@ struct PipeParams {
     uint2* staged;         // [totalTiles * chunkSize] (objectId, lodId)
     uint32_t* chunkCount;  // [totalTiles]
     unsigned int* workCounter;  // next chunk to decide (zero between launches), or NULL: static chunks
+    void* keep;            // kept frame: [totalTiles * chunkSize] survivors (32 bytes each) pass 1 keeps for pass 2
+    uint32_t* keepCount;   // kept frame: [totalTiles] survivors per chunk
+    uint2* staged2;        // fused frame: pass 1's staged records, [totalTiles * chunkSize]
+    uint32_t* chunkCount2; // fused frame: [totalTiles]
 };
 
 struct InstancedParams {
@@ -165,6 +181,9 @@ struct PyramidBuildParams {
     float* data;
     uint32_t width, height, mipCount, mode;
     uint32_t mipOffset[BLZ_PYRAMID_MAX_MIPS];
+    unsigned int* done;  // the context's finished-tile counter (zero between builds)
+    uint32_t vec4;       // D3D12: depth rows read 16 bytes at a time (width % 4 == 0, height >= 2, aligned buffers)
+    uint32_t pad;
 };
 
 // Launches a kernel with programmatic stream serialization: it may be scheduled while the kernel
@@ -194,6 +213,16 @@ uint32_t single_chunk_size(uint32_t mode, uint32_t threads, uint32_t opt, uint32
 bool single_shape_supported(uint32_t threads, uint32_t opt);
 cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t threads, uint32_t opt, int smCount,
                                cudaStream_t s);
+// A kept frame (blz_frame_first / blz_frame_late): pass 1 tests every object once and keeps the
+// frustum survivors in p.keep; pass 2 runs the pyramid test over those alone. `scatter` false leaves
+// the records staged.
+cudaError_t launch_frame_first(const PipeParams& p, uint32_t threads, uint32_t opt, int smCount, cudaStream_t s,
+                               bool scatter);
+cudaError_t launch_frame_late(const PipeParams& p, int smCount, cudaStream_t s, bool scatter);
+cudaError_t launch_frame_scatter2(const PipeParams& p1, const PipeParams& p2, cudaStream_t s);
+// The fused sweep of blz_cull_frame (kModeFrameFused) after the pyramid: p stages pass 2's records in
+// staged / chunkCount and pass 1's in staged2 / chunkCount2; no scatter.
+cudaError_t launch_frame_fused(const PipeParams& p, uint32_t threads, uint32_t opt, int smCount, cudaStream_t s);
 bool batch_shape_supported(uint32_t threads, uint32_t opt);
 // mode: the pass every view of the batch runs, or -1 when they differ (the kernel reads it per view)
 cudaError_t launch_batch_cull(const PipeParams& p, uint32_t threads, uint32_t opt, uint32_t blocksPerSm, int smCount,

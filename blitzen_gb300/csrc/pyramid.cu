@@ -1,13 +1,14 @@
-// pyramid.cu — single-pass Hi-Z depth pyramid.
+// pyramid.cu — single-launch Hi-Z depth pyramid.
 //
 // The reference builds the pyramid with one dispatch per mip and a barrier between them
 // (src/Renderer/BlitzenDX12/dx12Draw.cpp:248-277, src/Renderer/BlitzenVulkan/vulkanDraw.cpp:579-614).
-// Here two launches build every mip: in the first, each block owns a 32x32 tile of mip 0 (every load
-// of the tile issued before any is used), writes it, and reduces it through mips 1..5 in shared
-// memory (a 32-texel tile reaches 1 texel at mip 5); the second, one block, reads mip 5 into
-// shared memory when it fits and builds the few remaining small mips there. (A last-block-finishes
-// form in one launch measured slower: every block fenced its writes and 510 blocks queued on one
-// counter.)
+// Here one launch builds every mip: each block owns a 32x32 tile of mip 0 (every load of the tile
+// issued before any is used; D3D12 depth rows read 16 bytes at a time where the extent allows),
+// writes it, and reduces it through mips 1..5 in shared memory (a 32-texel tile reaches 1 texel at
+// mip 5). The block that finishes last (a counter in the context, taken after the block's mip-5
+// texel is fenced; no block waits) builds the few remaining small mips from mip 5 and rewinds the
+// counter. Pyramid builds of one context are therefore ordered on the device, as all of a context's
+// work is.
 //
 // Texel rules:
 //   D3D12   depthPyramid.cs.hlsl:16-26 — min(r, min(g, min(b, a))) of the 2x2 Loads at
@@ -23,11 +24,9 @@
 namespace blz {
 
 constexpr int kPyrThreads = 256;
-constexpr int kPyrTopThreads = 1024;
 constexpr uint32_t kPyrTile = 32;
 constexpr uint32_t kPyrInTileLevels = 5;
 constexpr uint32_t kPyrPerThread = kPyrTile * kPyrTile / kPyrThreads;  // mip-0 texels per thread
-constexpr uint32_t kPyrTopTexels = 4096;  // the last block keeps the upper levels in shared memory up to this
 
 __device__ __forceinline__ float load_or_zero(const float* img, uint32_t w, uint32_t h, uint64_t x, uint64_t y) {
     return (x < w && y < h) ? __ldcg(img + y * w + x) : 0.0f;
@@ -73,10 +72,74 @@ __device__ __forceinline__ float level_texel_global(const float* src, uint32_t s
     return m;
 }
 
+// The levels above the tiles' last (mip 5), built by one block from mip 5 in global memory: in
+// shared memory when mip 5 fits bufA (capA texels) and half of it fits bufB (capB texels) — each
+// level has at most half the texels of the one before (a quarter unless one side is already 1), so
+// the levels alternate between the two buffers — else level by level through global memory.
 template <uint32_t MODE>
-__global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuildParams p) {
+__device__ __forceinline__ void top_levels(const PyramidBuildParams& p, float* bufA, uint32_t capA, float* bufB,
+                                           uint32_t capB) {
+    const uint32_t W0 = p.width, H0 = p.height;
+    uint32_t k = kPyrInTileLevels + 1;
+    const uint32_t Wt = mip_dim(W0, kPyrInTileLevels), Ht = mip_dim(H0, kPyrInTileLevels);
+    if (Wt * Ht <= capA && Wt * Ht <= 2u * capB) {
+        const float* top = p.data + p.mipOffset[kPyrInTileLevels];
+        for (uint32_t i = threadIdx.x; i < Wt * Ht; i += kPyrThreads) bufA[i] = __ldcg(top + i);
+        __syncthreads();
+        float* prev = bufA;
+        float* next = bufB;
+        for (; k < p.mipCount; ++k) {
+            const uint32_t Wp = mip_dim(W0, k - 1), Hp = mip_dim(H0, k - 1);
+            const uint32_t Wk = mip_dim(W0, k), Hk = mip_dim(H0, k);
+            float* out = p.data + p.mipOffset[k];
+            for (uint32_t idx = threadIdx.x; idx < Wk * Hk; idx += kPyrThreads) {
+                const uint32_t gx = idx % Wk, gy = idx / Wk;
+                float t;
+                if (MODE == BLZ_HIZ_D3D12) {
+                    const uint32_t x0 = 2u * gx, y0 = 2u * gy;
+                    const float r = (x0 < Wp && y0 < Hp) ? prev[y0 * Wp + x0] : 0.0f;
+                    const float g = (x0 + 1 < Wp && y0 < Hp) ? prev[y0 * Wp + x0 + 1] : 0.0f;
+                    const float b = (x0 < Wp && y0 + 1 < Hp) ? prev[(y0 + 1) * Wp + x0] : 0.0f;
+                    const float a = (x0 + 1 < Wp && y0 + 1 < Hp) ? prev[(y0 + 1) * Wp + x0 + 1] : 0.0f;
+                    t = fmin_nan(r, fmin_nan(g, fmin_nan(b, a)));
+                } else {
+                    uint32_t i0, i1, j0, j1;
+                    vk_footprint(gx, Wk, Wp, i0, i1);
+                    vk_footprint(gy, Hk, Hp, j0, j1);
+                    float m = __int_as_float(0x7fc00000);
+                    m = fmin_nan(m, prev[j0 * Wp + i0]);
+                    m = fmin_nan(m, prev[j0 * Wp + i1]);
+                    m = fmin_nan(m, prev[j1 * Wp + i0]);
+                    m = fmin_nan(m, prev[j1 * Wp + i1]);
+                    t = m;
+                }
+                next[idx] = t;
+                out[idx] = t;
+            }
+            __syncthreads();
+            float* tmp = prev;
+            prev = next;
+            next = tmp;
+        }
+        return;
+    }
+    for (; k < p.mipCount; ++k) {
+        const uint32_t Wp = mip_dim(W0, k - 1), Hp = mip_dim(H0, k - 1);
+        const uint32_t Wk = mip_dim(W0, k), Hk = mip_dim(H0, k);
+        const float* prev = p.data + p.mipOffset[k - 1];
+        float* out = p.data + p.mipOffset[k];
+        for (uint32_t idx = threadIdx.x; idx < Wk * Hk; idx += kPyrThreads) {
+            const uint32_t gx = idx % Wk, gy = idx / Wk;
+            out[idx] = level_texel_global<MODE>(prev, Wp, Hp, gx, gy, Wk, Hk);
+        }
+        __syncthreads();  // this block's writes of level k are visible to its reads of level k + 1
+    }
+}
+
+template <uint32_t MODE>
+__global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const __grid_constant__ PyramidBuildParams p) {
     __shared__ float sA[kPyrTile * kPyrTile];
-    __shared__ float sB[(kPyrTile / 2) * (kPyrTile / 2)];
+    __shared__ float sB[kPyrTile * kPyrTile / 2];  // mip 1 of the tile (a quarter of it), or a top level
     pdl_wait();
     pdl_launch_next();
     const uint32_t X0 = blockIdx.x * kPyrTile, Y0 = blockIdx.y * kPyrTile;
@@ -85,7 +148,36 @@ __global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuild
     // mip 0 from the depth buffer: all of a thread's source loads are in flight together
     {
         float v[kPyrPerThread];
-        if (MODE == BLZ_HIZ_D3D12) {
+        if (MODE == BLZ_HIZ_D3D12 && p.vec4) {
+            // thread t takes the texel pairs (2i, 2i+1) of tile row j for the pair indices
+            // t, t + 256 (16 pairs per row): depth rows 2y and 2y+1, columns 4i .. 4i+3, one 16-byte
+            // load each. The host chose this path only for a depth width that is a multiple of 4 (so
+            // the mip-0 width is even and a pair never crosses it) and a 16-byte aligned buffer.
+            float4 q[kPyrPerThread / 2][2];
+            const uint32_t dw = p.depthWidth;
+#pragma unroll
+            for (uint32_t j = 0; j < kPyrPerThread / 2; ++j) {
+                const uint32_t pr = threadIdx.x + j * kPyrThreads;
+                const uint32_t gx = X0 + 2u * (pr % (kPyrTile / 2)), gy = Y0 + pr / (kPyrTile / 2);
+                const bool in = gx < W0 && gy < H0;
+                const float4* row = reinterpret_cast<const float4*>(p.depth + static_cast<size_t>(2u * gy) * dw + 2u * gx);
+                q[j][0] = in ? __ldg(row) : make_float4(0.f, 0.f, 0.f, 0.f);
+                q[j][1] = in ? __ldg(row + dw / 4u) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (uint32_t j = 0; j < kPyrPerThread / 2; ++j) {
+                const uint32_t pr = threadIdx.x + j * kPyrThreads;
+                const uint32_t lx = 2u * (pr % (kPyrTile / 2)), ly = pr / (kPyrTile / 2);
+                const uint32_t gx = X0 + lx, gy = Y0 + ly;
+                const bool in = gx < W0 && gy < H0;
+                // texel (2i): r = row0.x, g = row0.y, b = row1.x, a = row1.y; texel (2i+1): .z, .w
+                const float t0 = fmin_nan(q[j][0].x, fmin_nan(q[j][0].y, fmin_nan(q[j][1].x, q[j][1].y)));
+                const float t1 = fmin_nan(q[j][0].z, fmin_nan(q[j][0].w, fmin_nan(q[j][1].z, q[j][1].w)));
+                if (in) *reinterpret_cast<float2*>(p.data + p.mipOffset[0] + static_cast<size_t>(gy) * W0 + gx) = make_float2(t0, t1);
+                sA[ly * kPyrTile + lx] = in ? t0 : 0.0f;
+                sA[ly * kPyrTile + lx + 1u] = in ? t1 : 0.0f;
+            }
+        } else if (MODE == BLZ_HIZ_D3D12) {
             float q[kPyrPerThread][4];
 #pragma unroll
             for (uint32_t j = 0; j < kPyrPerThread; ++j) {
@@ -110,13 +202,15 @@ __global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuild
                                             : 0.0f;
             }
         }
+        if (!(MODE == BLZ_HIZ_D3D12 && p.vec4)) {
 #pragma unroll
-        for (uint32_t j = 0; j < kPyrPerThread; ++j) {
-            const uint32_t idx = threadIdx.x + j * kPyrThreads;
-            const uint32_t gx = X0 + (idx % kPyrTile), gy = Y0 + (idx / kPyrTile);
-            const bool in = gx < W0 && gy < H0;
-            if (in) p.data[p.mipOffset[0] + static_cast<size_t>(gy) * W0 + gx] = v[j];
-            sA[idx] = in ? v[j] : 0.0f;
+            for (uint32_t j = 0; j < kPyrPerThread; ++j) {
+                const uint32_t idx = threadIdx.x + j * kPyrThreads;
+                const uint32_t gx = X0 + (idx % kPyrTile), gy = Y0 + (idx / kPyrTile);
+                const bool in = gx < W0 && gy < H0;
+                if (in) p.data[p.mipOffset[0] + static_cast<size_t>(gy) * W0 + gx] = v[j];
+                sA[idx] = in ? v[j] : 0.0f;
+            }
         }
     }
     __syncthreads();
@@ -169,85 +263,30 @@ __global__ void __launch_bounds__(kPyrThreads) pyramid_kernel(const PyramidBuild
         S = Sk;
     }
 
-}
-
-// The mips above level 5, which span several tiles, by one block.
-template <uint32_t MODE>
-__global__ void __launch_bounds__(kPyrTopThreads) pyramid_top_kernel(const PyramidBuildParams p) {
-    __shared__ float sTop[2][kPyrTopTexels];
-    pdl_wait();
-    pdl_launch_next();
-    const uint32_t W0 = p.width, H0 = p.height;
-    uint32_t k = kPyrInTileLevels + 1;
-    {
-        // the level every tile finished, then the rest in shared memory while they fit
-        const uint32_t Wt = mip_dim(W0, kPyrInTileLevels), Ht = mip_dim(H0, kPyrInTileLevels);
-        if (Wt * Ht <= kPyrTopTexels) {
-            const float* top = p.data + p.mipOffset[kPyrInTileLevels];
-            for (uint32_t i = threadIdx.x; i < Wt * Ht; i += kPyrTopThreads) sTop[0][i] = __ldcg(top + i);
-            __syncthreads();
-            int cur = 0;
-            for (; k < p.mipCount; ++k) {
-                const uint32_t Wp = mip_dim(W0, k - 1), Hp = mip_dim(H0, k - 1);
-                const uint32_t Wk = mip_dim(W0, k), Hk = mip_dim(H0, k);
-                const float* prev = sTop[cur];
-                float* next = sTop[cur ^ 1];
-                float* out = p.data + p.mipOffset[k];
-                for (uint32_t idx = threadIdx.x; idx < Wk * Hk; idx += kPyrTopThreads) {
-                    const uint32_t gx = idx % Wk, gy = idx / Wk;
-                    float t;
-                    if (MODE == BLZ_HIZ_D3D12) {
-                        const uint32_t x0 = 2u * gx, y0 = 2u * gy;
-                        const float r = (x0 < Wp && y0 < Hp) ? prev[y0 * Wp + x0] : 0.0f;
-                        const float g = (x0 + 1 < Wp && y0 < Hp) ? prev[y0 * Wp + x0 + 1] : 0.0f;
-                        const float b = (x0 < Wp && y0 + 1 < Hp) ? prev[(y0 + 1) * Wp + x0] : 0.0f;
-                        const float a = (x0 + 1 < Wp && y0 + 1 < Hp) ? prev[(y0 + 1) * Wp + x0 + 1] : 0.0f;
-                        t = fmin_nan(r, fmin_nan(g, fmin_nan(b, a)));
-                    } else {
-                        uint32_t i0, i1, j0, j1;
-                        vk_footprint(gx, Wk, Wp, i0, i1);
-                        vk_footprint(gy, Hk, Hp, j0, j1);
-                        float m = __int_as_float(0x7fc00000);
-                        m = fmin_nan(m, prev[j0 * Wp + i0]);
-                        m = fmin_nan(m, prev[j0 * Wp + i1]);
-                        m = fmin_nan(m, prev[j1 * Wp + i0]);
-                        m = fmin_nan(m, prev[j1 * Wp + i1]);
-                        t = m;
-                    }
-                    next[idx] = t;
-                    out[idx] = t;
-                }
-                __syncthreads();
-                cur ^= 1;
-            }
+    if (p.mipCount > kPyrInTileLevels + 1) {
+        // the levels above 5 span several tiles: the last block to finish builds them. Thread 0
+        // wrote this tile's mip-5 texel; it fences it before counting the block done, and the last
+        // block fences again before reading every tile's texel
+        __shared__ unsigned int s_last;
+        if (threadIdx.x == 0) {
+            __threadfence();
+            s_last = atomicAdd(p.done, 1u) == gridDim.x * gridDim.y - 1u ? 1u : 0u;
         }
-    }
-    for (; k < p.mipCount; ++k) {  // levels too large for shared memory, through global memory
-        const uint32_t Wp = mip_dim(W0, k - 1), Hp = mip_dim(H0, k - 1);
-        const uint32_t Wk = mip_dim(W0, k), Hk = mip_dim(H0, k);
-        const float* prev = p.data + p.mipOffset[k - 1];
-        float* out = p.data + p.mipOffset[k];
-        for (uint32_t idx = threadIdx.x; idx < Wk * Hk; idx += kPyrTopThreads) {
-            const uint32_t gx = idx % Wk, gy = idx / Wk;
-            out[idx] = level_texel_global<MODE>(prev, Wp, Hp, gx, gy, Wk, Hk);
-        }
-        __threadfence_block();
         __syncthreads();
+        if (s_last) {
+            __threadfence();
+            top_levels<MODE>(p, sA, kPyrTile * kPyrTile, sB, kPyrTile * kPyrTile / 2);
+            if (threadIdx.x == 0) *p.done = 0u;  // rewound for the context's next build
+        }
     }
 }
 
 cudaError_t launch_pyramid_build(const PyramidBuildParams& p, cudaStream_t s, uint32_t* launches) {
     dim3 grid((p.width + kPyrTile - 1) / kPyrTile, (p.height + kPyrTile - 1) / kPyrTile);
-    const bool top = p.mipCount > kPyrInTileLevels + 1;
     cudaError_t e;
-    if (p.mode == BLZ_HIZ_VULKAN) {
-        e = launch_pdl(pyramid_kernel<BLZ_HIZ_VULKAN>, grid, dim3(kPyrThreads), 0, s, p);
-        if (e == cudaSuccess && top) e = launch_pdl(pyramid_top_kernel<BLZ_HIZ_VULKAN>, dim3(1), dim3(kPyrTopThreads), 0, s, p);
-    } else {
-        e = launch_pdl(pyramid_kernel<BLZ_HIZ_D3D12>, grid, dim3(kPyrThreads), 0, s, p);
-        if (e == cudaSuccess && top) e = launch_pdl(pyramid_top_kernel<BLZ_HIZ_D3D12>, dim3(1), dim3(kPyrTopThreads), 0, s, p);
-    }
-    if (launches) *launches += top ? 2u : 1u;
+    if (p.mode == BLZ_HIZ_VULKAN) e = launch_pdl(pyramid_kernel<BLZ_HIZ_VULKAN>, grid, dim3(kPyrThreads), 0, s, p);
+    else e = launch_pdl(pyramid_kernel<BLZ_HIZ_D3D12>, grid, dim3(kPyrThreads), 0, s, p);
+    if (launches) *launches += 1u;
     return e;
 }
 

@@ -238,6 +238,27 @@ class Culler:
         check(self.lib.blz_cull_late(self.ctx, C.byref(view), self._list(objects, count), visibility.data_ptr(),
                                      C.byref(pyramid.desc), C.byref(t), _stream_ptr(stream)), "blz_cull_late")
 
+    def frame_first_pass(self, view, visibility: torch.Tensor, target: Target, objects=None, count=None, stream=None):
+        """Pass 1 of a kept frame (blz_frame_first): pass 1's records, and the frustum survivors kept
+        for frame_occlusion_pass."""
+        t = target.ctype()
+        check(self.lib.blz_frame_first(self.ctx, C.byref(view), self._list(objects, count), visibility.data_ptr(),
+                                       C.byref(t), _stream_ptr(stream)), "blz_frame_first")
+
+    def frame_occlusion_pass(self, pyramid: DevicePyramid, target: Target, stream=None):
+        """Pass 2 of the kept frame (blz_frame_late): the kept survivors against the pyramid."""
+        t = target.ctype()
+        check(self.lib.blz_frame_late(self.ctx, C.byref(pyramid.desc), C.byref(t), _stream_ptr(stream)),
+              "blz_frame_late")
+
+    def cull_frame(self, view, visibility: torch.Tensor, depth: torch.Tensor, pyramid: DevicePyramid, target1: Target,
+                   target2: Target, objects=None, count=None, stream=None):
+        """Both occlusion passes and the pyramid of one frame in one call (blz_cull_frame)."""
+        a, b = target1.ctype(), target2.ctype()
+        check(self.lib.blz_cull_frame(self.ctx, C.byref(view), self._list(objects, count), visibility.data_ptr(),
+                                      depth.data_ptr(), C.byref(pyramid.desc), C.byref(a), C.byref(b),
+                                      _stream_ptr(stream)), "blz_cull_frame")
+
     def draw_cull_temporal(self, view, pyramid: DevicePyramid, target: Target, objects=None, count=None, stream=None):
         t = target.ctype()
         check(self.lib.blz_cull_temporal(self.ctx, C.byref(view), self._list(objects, count), C.byref(pyramid.desc),

@@ -242,6 +242,37 @@ int blz_cull_late(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList lis
                   uint32_t* dVisibility, const BlzPyramid* pyramid, const BlzCullTarget* target,
                   blz_stream_t stream);
 
+/* Kept frame: the two occlusion passes of one frame with the frustum work done once.
+ * The reference's frame is UpdateBuffers, pass 1, the pass-1 draw, the depth pyramid, pass 2
+ * (VulkanRenderer::DrawFrame, src/Renderer/BlitzenVulkan/vulkanDraw.cpp:830,1015-1031): both passes
+ * see the same view, transforms and render list. blz_frame_first runs pass 1 over every object of the
+ * list: it writes pass 1's records exactly as blz_cull_first does, and keeps every object inside the
+ * frustum (with its view-space sphere, in context memory) for blz_frame_late, which tests only those
+ * against the pyramid and writes pass 2's records exactly as blz_cull_late does. Together they leave
+ * the same records, counts and visibility as blz_cull_first + blz_cull_late.
+ * Contract: between the two calls the scene tables, bound dynamic rows, render list and visibility
+ * buffer must not change (the renderer's own frame guarantees this). blz_frame_first already writes
+ * the final visibility (0) of the objects it found outside the frustum; blz_frame_late rewrites the
+ * rest. blz_frame_late uses the last blz_frame_first of the context (BLZ_ERR_INVALID_ARGUMENT if
+ * there is none). Replaces DrawCullFirstPass / DrawCullOcclusionPass (vulkanDraw.cpp:107-226),
+ * drawOccFirst.cs.hlsl:13-58 and drawOccLate.cs.hlsl:13-67. */
+int blz_frame_first(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list, uint32_t* dVisibility,
+                    const BlzCullTarget* pass1Target, blz_stream_t stream);
+int blz_frame_late(blz_ctx* ctx, const BlzPyramid* pyramid, const BlzCullTarget* pass2Target, blz_stream_t stream);
+
+/* The whole frame in one call for a caller whose depth buffer is ready before pass 1 (an occluder
+ * depth pass, a reprojected previous depth): the pyramid is built from dDepth first, then one sweep
+ * tests every object once against the frustum and its survivors against the pyramid, and sorts each
+ * object into pass 1's records (visible last frame, inside the frustum), pass 2's (not visible last
+ * frame, inside the frustum, not occluded) or neither, rewriting the visibility as pass 2 does; one
+ * final launch writes both record lists. Same records, counts, pyramid and visibility as
+ * blz_cull_first + blz_pyramid_build + blz_cull_late on the same inputs. It keeps nothing for
+ * blz_frame_late. Replaces the pass order of VulkanRenderer::DrawFrame (vulkanDraw.cpp:1015-1031)
+ * and dx12Draw.cpp:590-641 minus the draws. */
+int blz_cull_frame(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list, uint32_t* dVisibility,
+                   const float* dDepth, const BlzPyramid* pyramid, const BlzCullTarget* pass1Target,
+                   const BlzCullTarget* pass2Target, blz_stream_t stream);
+
 /* Single-pass occlusion against a pyramid (last frame's), no visibility state.
  * Replaces drawOccTemporal.hlsl:13-64. */
 int blz_cull_temporal(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list,

@@ -115,3 +115,46 @@ def test_bench_frame_recorded_replays(bench_frame, stride):
         finally:
             g.close()
     assert c.check(side) == 0
+
+
+@pytest.mark.parametrize("stride", [abi.STRIDE_VULKAN, abi.STRIDE_D3D12])
+def test_bench_frame_kept_frame(bench_frame, stride):
+    """blz_frame_first, the pyramid, blz_frame_late: the renderer's frame order with pass 2 testing
+    only what pass 1 kept."""
+    c, sc, v, depth = bench_frame[:4]
+    vis, t1, t2, pyr = _frame_buffers(sc, stride)
+    c.frame_first_pass(v, vis, t1)
+    c.generate_depth_pyramid(pyr, depth)
+    c.frame_occlusion_pass(pyr, t2)
+    assert c.check() == 0
+    _check(bench_frame, stride, vis, t1, t2, pyr, "kept frame")
+
+
+@pytest.mark.parametrize("stride", [abi.STRIDE_VULKAN, abi.STRIDE_D3D12])
+def test_bench_frame_one_call_recorded(bench_frame, stride):
+    """blz_cull_frame directly, then recorded once and replayed three times (the bench's headline form)."""
+    c, sc, v, depth = bench_frame[:4]
+    vis, t1, t2, pyr = _frame_buffers(sc, stride)
+    vis0 = vis.clone()
+    c.cull_frame(v, vis, depth, pyr, t1, t2)
+    assert c.check() == 0
+    _check(bench_frame, stride, vis, t1, t2, pyr, "one call")
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        c.capture_begin()
+        c.cull_frame(v, vis, depth, pyr, t1, t2)
+        g = c.capture_end()
+        try:
+            for rep in range(3):
+                vis.copy_(vis0)
+                t1.count.fill_(0)
+                t2.count.fill_(0)
+                t1.commands.fill_(0)
+                t2.commands.fill_(0)
+                pyr.storage.fill_(-1.0)
+                g.launch()
+                side.synchronize()
+                _check(bench_frame, stride, vis, t1, t2, pyr, f"one call, replay {rep}")
+        finally:
+            g.close()
+    assert c.check(side) == 0

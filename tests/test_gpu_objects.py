@@ -150,8 +150,28 @@ def test_pyramid_odd_sizes(sculler, wh, mode):
     assert np.array_equal(p.storage.cpu().numpy().view(np.uint32), ref.data.view(np.uint32)), (w, h, mode)
 
 
+def run_frame(c, form, v, vis, depth, pyr, t1, t2, objects=None, count=None):
+    """One occlusion frame in one of the library's three forms: the separate calls (blz_cull_first,
+    blz_pyramid_build, blz_cull_late), the kept frame (blz_frame_first, blz_pyramid_build,
+    blz_frame_late) or the one call (blz_cull_frame)."""
+    if form == "calls":
+        c.draw_cull_first_pass(v, vis, t1, objects=objects, count=count)
+        c.generate_depth_pyramid(pyr, depth)
+        c.draw_cull_occlusion_pass(v, vis, pyr, t2, objects=objects, count=count)
+    elif form == "kept":
+        c.frame_first_pass(v, vis, t1, objects=objects, count=count)
+        c.generate_depth_pyramid(pyr, depth)
+        c.frame_occlusion_pass(pyr, t2)
+    else:
+        c.cull_frame(v, vis, depth, pyr, t1, t2, objects=objects, count=count)
+
+
+FORMS = ["calls", "kept", "one_call"]
+
+
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("hiz", [abi.HIZ_D3D12, abi.HIZ_VULKAN])
-def test_two_pass_occlusion(sculler, stress, hiz):
+def test_two_pass_occlusion(sculler, stress, hiz, form):
     sc, v, depth = stress
     if hiz == abi.HIZ_VULKAN:
         pl, _ = abi.pyramid_layout(W, H, hiz)
@@ -159,9 +179,7 @@ def test_two_pass_occlusion(sculler, stress, hiz):
     vis = torch.from_numpy(sc.visibility.view(np.int32).copy()).cuda()
     t1, t2 = Target.alloc(sc.count), Target.alloc(sc.count)
     p = DevicePyramid(W, H, hiz)
-    sculler.draw_cull_first_pass(v, vis, t1)
-    sculler.generate_depth_pyramid(p, torch.from_numpy(depth).cuda())
-    sculler.draw_cull_occlusion_pass(v, vis, p, t2)
+    run_frame(sculler, form, v, vis, torch.from_numpy(depth).cuda(), p, t1, t2)
     assert sculler.check() == 0
 
     ovis = sc.visibility.copy()
@@ -251,6 +269,58 @@ def test_capture_refuses_to_grow_scratch(culler, c1):
         g = culler.capture_end()
         g.close()
     assert ei.value.code == 2  # BLZ_ERR_CAPACITY
+
+
+@pytest.mark.parametrize("form", ["kept", "one_call"])
+def test_kept_frame_unusual_words_bad_ids_and_overflow(culler, c1, form):
+    """The kept frame against the oracle where the forms could part: visibility words other than 0/1
+    (any non-zero word is 'visible last frame', every word ends 0 or 1), out-of-range transform and
+    surface ids in a custom render list, and both outputs smaller than their record counts."""
+    v = view_for(zfar=1e4, yaw=0.3)
+    depth = O.depth_raster(v, S.make_occluders(np.random.default_rng(21), 400), W, H)
+    objs = c1.objects[::2].copy()
+    objs["surfaceId"][5] = 10_000
+    objs["transformId"][9] = 10_000_000
+    words = np.array([0, 1, 2, 0x80000000, 0xFFFFFFFF], np.uint32)
+    vis0 = words[np.random.default_rng(22).integers(0, len(words), len(objs))]
+    ovis = vis0.copy()
+    n1, r1, f1 = O.cull(1, v, c1, objects=objs, vis=ovis)
+    n2, r2, f2 = O.cull(2, v, c1, objects=objs, vis=ovis, pyramid=O.pyramid_build(depth))
+    assert (f1 | f2) & abi.FLAG_BAD_INDEX
+    dev = to_device(objs, "cuda")
+    for cap1, cap2 in ((len(objs), len(objs)), (n1 // 2, n2 // 3)):
+        vis = torch.from_numpy(vis0.view(np.int32).copy()).cuda()
+        t1, t2 = Target.alloc(cap1), Target.alloc(cap2)
+        pyr = DevicePyramid(W, H)
+        run_frame(culler, form, v, vis, torch.from_numpy(depth).cuda(), pyr, t1, t2, objects=dev, count=len(objs))
+        flags = culler.flags()
+        assert flags & abi.FLAG_BAD_INDEX
+        assert bool(flags & abi.FLAG_COMMAND_OVERFLOW) == (cap1 < n1 or cap2 < n2)
+        assert_records_equal(t1.read(), (n1, r1[:cap1]), f"{form} pass 1, capacity {cap1}")
+        assert_records_equal(t2.read(), (n2, r2[:cap2]), f"{form} pass 2, capacity {cap2}")
+        assert np.array_equal(vis.cpu().numpy().view(np.uint32), ovis)
+
+
+def test_kept_frame_empty_list_and_missing_first(culler, c1):
+    v = view_for()
+    vis = torch.zeros(4, dtype=torch.int32, device="cuda")
+    t1, t2 = Target.alloc(4), Target.alloc(4)
+    t1.count.fill_(7)
+    t2.count.fill_(7)
+    pyr = DevicePyramid(W, H)
+    depth = torch.zeros(W * H, dtype=torch.float32, device="cuda")
+    culler.cull_frame(v, vis, depth, pyr, t1, t2, objects=torch.zeros(2, dtype=torch.int32, device="cuda"), count=0)
+    assert culler.check() == 0
+    assert t1.read()[0] == 0 and t2.read()[0] == 0
+    from blitzen_gb300.culler import Culler
+    fresh = Culler(0)
+    try:
+        fresh.setup_for_rendering(c1)
+        with pytest.raises(abi.BlzError) as ei:
+            fresh.frame_occlusion_pass(pyr, t2)
+        assert ei.value.code == 1
+    finally:
+        fresh.close()
 
 
 def test_late_pass_with_unusual_visibility_words(culler, c1):
