@@ -164,6 +164,8 @@ _PROTOS = {
     "blz_last_error": (C.c_char_p, []),
     "blz_version": (C.c_char_p, []),
     "blz_ctx_check": (_I, [_P, _P, C.POINTER(_U32)]),
+    "blz_ctx_set_wait_limit": (_I, [_P, _U32]),
+    "blz_ctx_debug_advance_ticket": (_I, [_P, _U32, _P]),
     "blz_ctx_launch_count": (C.c_uint64, [_P]),
     "blz_scene_upload": (_I, [_P, C.POINTER(SceneDesc), _U32, _P]),
     "blz_scene_device_tables": (_I, [_P, C.POINTER(SceneDesc)]),

@@ -236,6 +236,20 @@ int blz_ctx_destroy(blz_ctx* c) {
 
 uint64_t blz_ctx_launch_count(const blz_ctx* c) { return c ? c->launches.load() : 0; }
 
+int blz_ctx_set_wait_limit(blz_ctx* c, uint32_t polls) {
+    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    c->waitLimit = polls ? polls : static_cast<uint32_t>(kSpinLimitDefault);
+    return BLZ_OK;
+}
+
+int blz_ctx_debug_advance_ticket(blz_ctx* c, uint32_t n, blz_stream_t stream) {
+    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (n == 0 || n > 1024) return fail(BLZ_ERR_INVALID_ARGUMENT, "ticket advance %u outside [1, 1024]", n);
+    cudaError_t e = launch_add_word(&c->scratch->ticket, n, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "ticket advance");
+    return BLZ_OK;
+}
+
 int blz_ctx_check(blz_ctx* c, blz_stream_t stream, uint32_t* flagsOut) {
     if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -840,6 +854,7 @@ int blz_cull_instanced(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList 
     p.capacity = target->capacity;
     p.drawCount = target->drawCount;
     p.scratch = c->scratch;
+    p.spinLimit = c->waitLimit;
     cudaError_t e = launch_instanced_cull(p, *view, reinterpret_cast<cudaStream_t>(s));
     if (e != cudaSuccess) return cuda_fail(e, "instanced cull launch");
     c->launches++;

@@ -47,6 +47,7 @@ struct blz_ctx {
     uint64_t launchesAtCapture = 0;
     BlzLaunchShape shape{256, 2, 0, 0};   // batch launches
     uint32_t singleThreads = 256, singleOpt = 2;  // single-view launches
+    uint32_t waitLimit = static_cast<uint32_t>(blz::kSpinLimitDefault);  // polls before a device-side wait gives up
     unsigned char* noallocBase = nullptr;  // device address of the no-alloc staging array, fetched by this context's first no-alloc call
     // kept frame (blz_frame_first / blz_frame_late): staged records of both passes, their chunk
     // counts, the survivors pass 1 keeps and their counts, and what pass 2 reuses of pass 1's call

@@ -294,7 +294,6 @@ struct Scratch {
 constexpr uint32_t kStateAggregate = 1u;
 constexpr uint32_t kStatePrefix = 2u;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
-constexpr unsigned long long kSpinLimit = 1ull << 20;  // bounded waits: about a second at worst
 
 __device__ __forceinline__ unsigned long long pack_state(uint32_t epoch, uint32_t flag, uint32_t value) {
     return (static_cast<unsigned long long>(epoch) << 32) | (static_cast<unsigned long long>(flag) << 30) |

@@ -67,6 +67,21 @@ __global__ void __launch_bounds__(kInstThreads) cull_instanced_kernel(const Inst
     __syncthreads();
     const uint32_t tile = s_tile, epoch = s_epoch;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    if (tile >= gridDim.x) {
+        // a ticket past the grid: the protocol state was left behind by a launch that gave up on a
+        // wait; this block touches no tile state and only takes part in the exit protocol
+        if (threadIdx.x == 0) {
+            atomicOr(&scr->status, BLZ_FLAG_TIMEOUT);
+            __threadfence();
+            if (atomicAdd(&scr->doneBlocks, 1u) == gridDim.x - 1u) {
+                scr->ticket = 0u;
+                scr->doneBlocks = 0u;
+                __threadfence();
+                atomicExch(&scr->epoch, epoch + 1u);
+            }
+        }
+        return;
+    }
     const ViewConsts v = load_view(view);
     // warp w owns objects [base + w*32*OPT, base + (w+1)*32*OPT), visited k-major (coalesced)
     const uint32_t wbase = tile * kInstTile + warp * 32u * kInstOpt;
@@ -116,7 +131,7 @@ __global__ void __launch_bounds__(kInstThreads) cull_instanced_kernel(const Inst
                 const uint32_t lo = static_cast<uint32_t>(s);
                 const uint32_t flag = (static_cast<uint32_t>(s >> 32) == epoch) ? (lo >> 30) : 0u;
                 if (flag == 0u) {
-                    if (++spins > kSpinLimit) {
+                    if (++spins > p.spinLimit) {
                         atomicOr(&scr->status, BLZ_FLAG_TIMEOUT);
                         break;
                     }

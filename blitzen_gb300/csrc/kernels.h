@@ -66,6 +66,7 @@ constexpr int kModeFrameFused = 5;
 constexpr int kObjThreads = 256;
 constexpr int kObjOpt = 2;
 constexpr uint32_t kMaxTiles = 1u << 20;             // tile states held by one scratch
+constexpr unsigned long long kSpinLimitDefault = 1ull << 20;  // polls of one state before a device-side wait gives up
 constexpr size_t kScratchHeaderBytes = 128;          // Scratch fields before the state array
 
 // Device copy of one view of a cull launch (its uniform, render list, mode, buffers).
@@ -123,6 +124,8 @@ struct InstancedParams {
     uint32_t* drawCount;
     uint32_t* lodBlockCounts;   // scratch: [tiles][lodCount] per-tile LOD histograms
     Scratch* scratch;
+    uint32_t spinLimit;         // polls of a state before the look-back gives up (BLZ_FLAG_TIMEOUT)
+    uint32_t pad1;
 };
 
 // The instanced cull's stages after the FRUSTUM decide kernel (see cull_objects.cu).
@@ -243,6 +246,8 @@ cudaError_t launch_transforms_scatter(BlzMeshTransform* table, uint32_t tableCou
 cudaError_t launch_transforms_rotate(const BlzMeshTransform* table, uint32_t tableCount, const BlzMeshTransform* dynRows,
                                      uint32_t dynCount, const uint32_t* ids, const float* axes, float angle, uint32_t n,
                                      BlzMeshTransform* dst, unsigned int* status, cudaStream_t s);
+// *word += n on the stream (one thread).
+cudaError_t launch_add_word(unsigned int* word, unsigned int n, cudaStream_t s);
 // *out = atomicExch(status, 0) on the stream (one thread).
 cudaError_t launch_take_status(unsigned int* status, unsigned int* out, cudaStream_t s);
 cudaError_t launch_depth_raster(const BlzCameraViewData& view, const float* boxes, uint32_t boxCount, float* depth,

@@ -156,6 +156,13 @@ namespace blz {
 
 __global__ void take_status_kernel(unsigned int* status, unsigned int* out) { *out = atomicExch(status, 0u); }
 
+__global__ void add_word_kernel(unsigned int* word, unsigned int n) { atomicAdd(word, n); }
+
+cudaError_t launch_add_word(unsigned int* word, unsigned int n, cudaStream_t s) {
+    add_word_kernel<<<1, 1, 0, s>>>(word, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_take_status(unsigned int* status, unsigned int* out, cudaStream_t s) {
     take_status_kernel<<<1, 1, 0, s>>>(status, out);
     return cudaGetLastError();

@@ -332,6 +332,14 @@ class Culler:
         self.lib.blz_ctx_check(self.ctx, _stream_ptr(stream), C.byref(f))
         return int(f.value)
 
+    def set_wait_limit(self, polls: int) -> None:
+        """Polls of one state before a device-side wait gives up (0: the default)."""
+        check(self.lib.blz_ctx_set_wait_limit(self.ctx, polls), "blz_ctx_set_wait_limit")
+
+    def debug_advance_ticket(self, n: int, stream=None) -> None:
+        """Test hook: the next ticket-taking launch starts past n places, so its waits run out."""
+        check(self.lib.blz_ctx_debug_advance_ticket(self.ctx, n, _stream_ptr(stream)), "blz_ctx_debug_advance_ticket")
+
     @property
     def launches(self) -> int:
         return int(self.lib.blz_ctx_launch_count(self.ctx))

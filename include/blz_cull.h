@@ -91,6 +91,22 @@ const char* blz_version(void);
  * the validation it never had (vulkanData.h:196-197). */
 int blz_ctx_check(blz_ctx* ctx, blz_stream_t stream, uint32_t* flagsOut);
 
+/* Bound of the device-side waits of this context's launches. The one kernel that waits is the
+ * single-kernel instanced cull (scenes of more than 1,024 LODs): a tile waits, per LOD, for the
+ * running totals of the tiles that started before it, polling one state at most `polls` times;
+ * then it gives up, raises BLZ_FLAG_TIMEOUT and finishes without waiting (its results are then
+ * wrong; blz_ctx_check returns BLZ_ERR_TIMEOUT and resets the protocol). 0 restores the default
+ * (2^20 polls, about a second at worst). Stands in for the bounded fence wait of the reference's
+ * frame loop (vulkanData.h:196-197, ce_fenceTimeout). */
+int blz_ctx_set_wait_limit(blz_ctx* ctx, uint32_t polls);
+
+/* Test hook for the timeout path only: advances the context's block-ticket counter by n (1..1024)
+ * on the stream, so that the next launch that takes tickets starts its blocks past the first n
+ * places. Its blocks then wait for places no block holds, give up after the wait limit and raise
+ * BLZ_FLAG_TIMEOUT; the launch's last block rewinds the counter, so the launch after it is whole
+ * again. No counterpart in the reference. */
+int blz_ctx_debug_advance_ticket(blz_ctx* ctx, uint32_t n, blz_stream_t stream);
+
 /* Number of this library's kernel launches enqueued by the context so far. */
 uint64_t blz_ctx_launch_count(const blz_ctx* ctx);
 

@@ -242,7 +242,7 @@ def test_recorded_frame_replays_match_direct_calls(culler, c1):
         culler.draw_cull_occlusion_pass(v, vis, pyr, t2)
         g = culler.capture_end()
         try:
-            assert g.kernels >= 5
+            assert g.kernels >= 3  # pass 1, pyramid, pass 2
             for rep in range(3):
                 vis.copy_(torch.from_numpy(vis0.view(np.int32).copy()).cuda())
                 t1.count.fill_(0)
