@@ -464,12 +464,16 @@ __device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_
         const uint32_t i = lane + 32u * u;
         preLod[u] = i < myN ? __ldg(reinterpret_cast<const uint2*>(p.sc.lods + pre[u].y)) : make_uint2(0u, 0u);
     }
-    // 1. records of the first chunk's view before c0
+    // 1. records of the first chunk's view before c0; each warp also hands its chunk's count to
+    //    warp 0 through shared memory
     uint32_t part = 0;
     for (uint32_t c = viewStart0 + threadIdx.x; c < c0; c += kScatterWarps * 32) part += __ldcg(p.chunkCount + c);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
-    if (lane == 0) s_part[warp] = part;
+    if (lane == 0) {
+        s_part[warp] = part;
+        s_n[warp] = myN;
+    }
     __syncthreads();
     // 2. warp 0: exclusive offsets of the block's chunks, a scan restarting at each view's first chunk
     if (warp == 0) {
@@ -478,7 +482,7 @@ __device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_
         for (int w = 0; w < kScatterWarps; ++w) carry += s_part[w];
         const uint32_t c = c0 + lane;
         const bool in = c < p.totalTiles;
-        const uint32_t n = in ? __ldcg(p.chunkCount + c) : 0u;
+        const uint32_t n = s_n[lane];  // 0 past the last chunk
         uint32_t vi = vi0;
         bool starts = false;  // this chunk starts a view (the scan restarts here)
         if constexpr (!SINGLE) {
@@ -509,7 +513,6 @@ __device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_
         // lanes still in the first view (no start at or before them) add the view's earlier records
         const uint32_t excl = sum - n + (flag ? 0u : carry);
         s_base[lane] = excl;
-        s_n[lane] = n;
         s_vi[lane] = vi;
         if (in) {
             const bool lastOfView = SINGLE ? (c + 1 == p.totalTiles) : (c + 1 == __ldg(p.tileStart + vi + 1));

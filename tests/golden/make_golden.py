@@ -19,6 +19,16 @@ Files (numpy .npz, compressed):
                  cull kinds: draw count, 32-byte records, visibility after the pass
   kat.npz        the boundary-case scene with a constant-per-mip pyramid, 4 cull kinds
   instanced.npz  the random scene's instanced cull: counters, instance ids, records
+  vkpyramid.npz  depth buffers and the reference's Vulkan pyramid of each (DepthPyramidGeneration
+                 .comp.glsl dispatched per level as vulkanDraw.cpp:554-622 does)
+  vkcull.npz     the random scene, 4 cameras x 3 Vulkan culls (TransparentDrawCull, InitialDrawCull,
+                 LateDrawCull against the Vulkan pyramid): draw count, 24-byte records, visibility
+  vkkat.npz      spheres one ulp either side of every Hi-Z level change of the Vulkan form, against
+                 constant-per-mip pyramids (LateDrawCull), with visibility
+  vkclusters.npz a cluster scene through PreClusterDrawCull + InitialClusterCull: dispatch entries and
+                 records (the reference runs no per-cluster test: its cone test is commented out)
+The Vulkan outputs come from the reference's GLSL compiled as C++ (oracle/ref_glsl/); the sampler's
+MIN-footprint is the one definition there that is not the reference's text (glsl_shim.h).
 
 Usage: python tests/golden/make_golden.py   (rebuilds oracle/_ref from the reference first)
 """
@@ -58,6 +68,19 @@ def ref_libs():
     hl.ref_hlsl_instanced.argtypes = [P, P, P, U, P, P, U, P, U]
     hl.ref_hlsl_instanced.restype = U
     return cam, hl
+
+
+def glsl_lib():
+    lib = ref_build.build_glsl()
+    if not lib:
+        raise SystemExit("the reference tree is not available: nothing to generate from")
+    gl = C.CDLL(str(lib))
+    gl.ref_glsl_cull.argtypes = [C.c_int, P, P, P, U, P, P, P]
+    gl.ref_glsl_cull.restype = U
+    gl.ref_glsl_pyramid.argtypes = [P, U, U, P]
+    gl.ref_glsl_clusters.argtypes = [P, P, P, U, P, P, P]
+    gl.ref_glsl_clusters.restype = U
+    return gl
 
 
 def ref_view(cam, fov, w, h, zn, zf, pos, yaw, pitch, pw, ph) -> abi.CameraViewData:
@@ -368,6 +391,146 @@ def kat_outputs(hl, out, sc, view, vis, pyrs) -> None:
                 out[f"vis_{pname}_{kind}"] = vis_out
 
 
+# ------------------------------------------------------------------ Vulkan form (GLSL)
+
+
+def vk_ref_pyramid(gl, depth: np.ndarray) -> O.HostPyramid:
+    h, w = depth.shape
+    p = O.HostPyramid(w, h, abi.HIZ_VULKAN)
+    gl.ref_glsl_pyramid(np.ascontiguousarray(depth, np.float32).ctypes.data, w, h, C.byref(p.desc))
+    return p
+
+
+def make_vk_pyramid(gl) -> dict:
+    rng = np.random.default_rng(505)
+    out = {}
+    shapes = [(1, 3), (2, 2), (5, 7), (48, 64), (199, 333), (37, 1000)]
+    depths = []
+    for h, w in shapes:
+        d = rng.random((h, w), dtype=np.float32)
+        d[rng.random((h, w)) < 0.3] = 0.0  # cleared depth
+        depths.append(d)
+    # an occluder raster of the stress camera at 640 x 360 (mip 0 512 x 256)
+    v = abi.view_setup(S.fov_radians(), 640.0, 360.0, S.ZNEAR, 1e4, (0.0, 0.0, 0.0), 0.0, 0.0, 512.0, 256.0)
+    depths.append(O.depth_raster(v, S.make_occluders(np.random.default_rng(506), 300), 640, 360))
+    for i, d in enumerate(depths):
+        p = vk_ref_pyramid(gl, d)
+        out[f"depth{i}"] = d
+        out[f"pyr{i}"] = p.data.copy()
+        out[f"mips{i}"] = np.array([p.desc.mipCount, p.desc.width, p.desc.height], np.uint32)
+    out["count"] = np.array([len(depths)], np.uint32)
+    return out
+
+
+def run_vk_cull(gl, kind: int, view, scene, vis, pyr) -> tuple[int, np.ndarray, np.ndarray | None]:
+    d, keep = O.scene_desc(scene)
+    n = scene.count
+    cmds = np.zeros((max(n, 1), 6), np.uint32)
+    v = None if vis is None else np.ascontiguousarray(vis.copy(), np.uint32)
+    cnt = gl.ref_glsl_cull(kind, C.byref(view), C.byref(d), keep[0].ctypes.data, n,
+                           None if v is None else v.ctypes.data, C.byref(pyr.desc) if pyr else None, cmds.ctypes.data)
+    return int(cnt), cmds[:cnt].copy(), v
+
+
+def make_vk_cull(cam, gl) -> dict:
+    sc = S.stress_scene(3000, seed=303, n_meshes=24, extent=300.0, n_boxes=200)
+    sc.transforms["scale"][5] = 0.0
+    sc.transforms["orientation"][6] = np.array([0.5, 0.5, 0.5, 0.9], np.float32)
+    fov = S.fov_radians()
+    pw, ph = 256.0, 128.0  # the Vulkan pyramid of a 320 x 180 depth buffer
+    views = [ref_view(cam, fov, 1920.0, 1080.0, 0.1, 1e4, (0.0, 0.0, 0.0), 0.0, 0.0, pw, ph),
+             ref_view(cam, fov, 1920.0, 1080.0, 0.1, 650.0, (20.0, -10.0, -300.0), 0.3, 0.1, pw, ph),
+             ref_view(cam, fov, 1920.0, 1080.0, 0.1, 1e30, (0.0, 50.0, 0.0), 2.0, -0.4, pw, ph),
+             ref_view(cam, fov, 1920.0, 1080.0, 0.1, 1e4, (0.0, 0.0, 0.0), 3.14159265, 0.0, pw, ph)]
+    out = scene_arrays("", sc)
+    out["visibility"] = sc.visibility
+    out["views"] = np.stack([vbytes(v) for v in views])
+    for c, v in enumerate(views):
+        depth = O.depth_raster(v, sc.boxes, 320, 180)
+        pyr = vk_ref_pyramid(gl, depth)
+        out[f"depth{c}"] = depth
+        out[f"pyr{c}"] = pyr.data.copy()
+        for kind in range(3):
+            vis = sc.visibility if kind in (1, 2) else None
+            cnt, cmds, vis_out = run_vk_cull(gl, kind, v, sc, vis, pyr if kind == 2 else None)
+            out[f"count{c}_{kind}"] = np.array([cnt], np.uint32)
+            out[f"cmds{c}_{kind}"] = cmds
+            if vis_out is not None:
+                out[f"vis{c}_{kind}"] = vis_out
+    return out
+
+
+def vk_constant_pyramid(width, height, values) -> O.HostPyramid:
+    p = O.HostPyramid(width, height, abi.HIZ_VULKAN)
+    for lvl in range(p.desc.mipCount):
+        p.mip(lvl)[:] = values[lvl % len(values)]
+    return p
+
+
+def make_vk_kat(cam, gl) -> dict:
+    """Spheres at every Hi-Z level change of the Vulkan form: level = floor(log2(max extent)) in
+    pyramid texels, clamped to [0, 16] by the sampler and to the last mip by the image. With
+    constant-per-mip pyramids the footprint does not matter, so the reference's own level choice and
+    clamping decide every answer."""
+    znear = 0.1
+    pw, ph = 1024.0, 1024.0  # the Vulkan pyramid of a 1920 x 1080 depth buffer
+    view = ref_view(cam, S.fov_radians(), 1920.0, 1080.0, znear, 1e4, (0.0, 0.0, 0.0), 0.0, 0.0, pw, ph)
+    pyr_alt = vk_constant_pyramid(1920, 1080, [0.0, 1.0])   # even mips pass, odd mips occlude
+    pyr_top = vk_constant_pyramid(1920, 1080, [0.0] * 9 + [1.0])  # only the last mip (9) occludes
+    k = KatScene()
+    ulps = (-2, -1, 0, 1, 2)
+    for pyr in (pyr_alt, pyr_top):
+        for z, x in ((100.0, 0.0), (37.5, 11.0), (400.0, -60.0), (12.0, 2.0)):
+            def vis(r, z=z, x=x, pyr=pyr):
+                return k.probe(view, 3, pyr, pos=(x, 0.0, z), radius=r)[0] > 0
+            rs = np.geomspace(0.001, z * 0.9, 2000).astype(np.float32)
+            vals = [vis(float(r)) for r in rs]
+            for i in range(1, len(rs)):
+                if vals[i] != vals[i - 1]:
+                    b = bisect(vis, float(rs[i - 1]), float(rs[i]))
+                    for u in ulps:
+                        k.add(pos=(x, 0.0, z), radius=_val(b + u))
+    # spheres whose projection spans the whole screen (level past the chain) and ones right at zNear
+    for r in (5.0, 50.0, 400.0):
+        k.add(pos=(0.0, 0.0, r + 0.5), radius=r)
+    sc = k.scene()
+    vis0 = np.zeros(sc.count, np.uint32)  # nothing visible last frame: every visible object is emitted
+    out = scene_arrays("", sc)
+    out["view"] = vbytes(view)
+    for name, pyr in (("alt", pyr_alt), ("top", pyr_top)):
+        cnt, cmds, vis_out = run_vk_cull(gl, 2, view, sc, vis0, pyr)
+        out[f"pyr_{name}"] = pyr.data.copy()
+        out[f"count_{name}"] = np.array([cnt], np.uint32)
+        out[f"cmds_{name}"] = cmds
+        out[f"vis_{name}"] = vis_out
+    return out, sc.count
+
+
+def make_vk_clusters(cam, gl) -> dict:
+    """A cluster scene whose clusters every per-cluster test of the library lets through (cluster
+    spheres of radius 1e6, a zero cone axis with cutoff 127): the library's cluster cull then emits
+    what the reference's object stage expands, and both are compared with these records."""
+    sc = S.cluster_scene(600, seed=606, n_meshes=8, clusters_per_mesh=24, extent=200.0)
+    sc.clusters["radius"] = np.float32(1e6)
+    sc.clusters["coneAxis"] = 0
+    sc.clusters["coneCutoff"] = 127
+    v = ref_view(cam, S.fov_radians(), 1920.0, 1080.0, 0.1, 1e4, (0.0, 0.0, -50.0), 0.2, 0.05, 960.0, 540.0)
+    d, keep = O.scene_desc(sc)
+    cap = int(sc.lods["clusterCount"].max()) * sc.count
+    dispatch = np.zeros((cap, 3), np.uint32)
+    cmds = np.zeros((cap, 6), np.uint32)
+    entries = C.c_uint32(0)
+    cnt = gl.ref_glsl_clusters(C.byref(v), C.byref(d), keep[0].ctypes.data, sc.count, dispatch.ctypes.data,
+                               C.byref(entries), cmds.ctypes.data)
+    out = scene_arrays("", sc)
+    out["clusters"] = sc.clusters
+    out["view"] = vbytes(v)
+    out["count"] = np.array([cnt], np.uint32)
+    out["cmds"] = cmds[:cnt].copy()
+    out["dispatch"] = dispatch[:entries.value].copy()
+    return out
+
+
 def main():
     cam, hl = ref_libs()
     np.savez_compressed(HERE / "camera.npz", **make_camera(cam))
@@ -377,9 +540,15 @@ def main():
     out, sc, view, vis, pyrs = make_kat(cam)
     kat_outputs(hl, out, sc, view, vis, pyrs)
     np.savez_compressed(HERE / "kat.npz", **out)
+    gl = glsl_lib()
+    np.savez_compressed(HERE / "vkpyramid.npz", **make_vk_pyramid(gl))
+    np.savez_compressed(HERE / "vkcull.npz", **make_vk_cull(cam, gl))
+    vk_out, vk_n = make_vk_kat(cam, gl)
+    np.savez_compressed(HERE / "vkkat.npz", **vk_out)
+    np.savez_compressed(HERE / "vkclusters.npz", **make_vk_clusters(cam, gl))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
-    print("kat objects", sc.count)
+    print("kat objects", sc.count, "vulkan kat objects", vk_n)
 
 
 if __name__ == "__main__":

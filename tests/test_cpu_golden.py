@@ -110,3 +110,74 @@ def test_oracle_threads_do_not_change_results():
     one = O.cull(3, v, sc, pyramid=pyr, stride=24, threads=1)
     many = O.cull(3, v, sc, pyramid=pyr, stride=24, threads=7)
     assert one[0] == many[0] and np.array_equal(one[1], many[1])
+
+
+# ----------------------------------------------------------------------------- Vulkan form (GLSL)
+# Fixtures from the reference's GLSL shaders compiled as C++ (oracle/ref_glsl/): everything but the
+# depth sampler's MIN footprint is the reference's own text there.
+
+VK_KINDS = {0: "frustum (TransparentDrawCull)", 1: "pass 1 (InitialDrawCull)", 2: "pass 2 (LateDrawCull)"}
+
+
+def _vk_host_pyramid(data: np.ndarray, depth_w: int, depth_h: int) -> O.HostPyramid:
+    p = O.HostPyramid(depth_w, depth_h, abi.HIZ_VULKAN)
+    assert p.data.size == data.size
+    p.data[:] = data
+    return p
+
+
+def test_vulkan_pyramid_oracle_matches_reference():
+    """DepthPyramidGeneration.comp.glsl dispatched per level (vulkanDraw.cpp:554-622): PreviousPow2
+    extent, the MIN sampler at (pos + 0.5) / levelExtent."""
+    d = G.load("vkpyramid")
+    for i in range(int(d["count"][0])):
+        depth = d[f"depth{i}"]
+        p = O.pyramid_build(depth, abi.HIZ_VULKAN)
+        assert [p.desc.mipCount, p.desc.width, p.desc.height] == list(d[f"mips{i}"])
+        assert np.array_equal(p.data.view(np.uint32), d[f"pyr{i}"].view(np.uint32)), f"pyramid {depth.shape}"
+
+
+@pytest.mark.parametrize("cam", range(4))
+@pytest.mark.parametrize("kind", range(3))
+def test_vulkan_cull_oracle_matches_reference(cam, kind):
+    d = G.load("vkcull")
+    sc = G.scene(d)
+    v = G.view(d["views"][cam])
+    pyr = _vk_host_pyramid(d[f"pyr{cam}"], 320, 180) if kind == 2 else None
+    vis = sc.visibility.copy() if kind in (1, 2) else None
+    n, recs, flags = O.cull(kind, v, sc, vis=vis, pyramid=pyr, stride=24)
+    assert flags == 0
+    _cmp((n, recs), int(d[f"count{cam}_{kind}"][0]), d[f"cmds{cam}_{kind}"], f"camera {cam} {VK_KINDS[kind]}")
+    if kind in (1, 2):
+        assert np.array_equal(vis, d[f"vis{cam}_{kind}"]), "visibility after the pass"
+
+
+@pytest.mark.parametrize("pyr_name", ["alt", "top"])
+def test_vulkan_boundary_cases_oracle_matches_reference(pyr_name):
+    """Spheres one ulp either side of every level change of the Vulkan Hi-Z (LateDrawCull with the
+    reference's level choice and LOD clamping), against constant-per-mip pyramids."""
+    d = G.load("vkkat")
+    sc = G.scene(d)
+    v = G.view(d["view"])
+    pyr = _vk_host_pyramid(d[f"pyr_{pyr_name}"], 1920, 1080)
+    vis = np.zeros(len(sc.objects), np.uint32)
+    n, recs, flags = O.cull(2, v, sc, vis=vis, pyramid=pyr, stride=24)
+    assert flags == 0
+    _cmp((n, recs), int(d[f"count_{pyr_name}"][0]), d[f"cmds_{pyr_name}"], f"vulkan boundary {pyr_name}")
+    assert np.array_equal(vis, d[f"vis_{pyr_name}"])
+    assert 0 < n < len(sc.objects)  # both answers occur
+
+
+def test_vulkan_cluster_records_oracle_matches_reference():
+    """PreClusterDrawCull + InitialClusterCull: the chosen LOD's clusters of every object inside the
+    frustum, records {objectId, triangleCount * 3, 1, dataOffset, 0, 0} in dispatch order. The scene's
+    clusters pass every per-cluster test of the oracle (the reference runs none)."""
+    d = G.load("vkclusters")
+    sc = G.scene(d)
+    sc.clusters = d["clusters"]
+    v = G.view(d["view"])
+    n, recs, ids, flags = O.cull_clusters(v, sc, stride=24)
+    assert flags == 0
+    _cmp((n, recs), int(d["count"][0]), d["cmds"], "cluster records")
+    assert np.array_equal(ids, d["dispatch"][:, 2]), "cluster ids"
+    assert np.array_equal(recs[:, 0], d["dispatch"][:, 0]), "object ids"
