@@ -132,15 +132,16 @@ def batched_views(culler, scene, device, n_views=64, reps=20, shape=None) -> dic
     }
 
 
-def serving(culler, scene, device, seconds=3.0, rate=2000.0, seed=0) -> dict:
+def _serve_run(culler, scene, n_req, seed, arrivals=None, max_outstanding=None) -> dict:
+    """One run of the request loop over the resident scene: n_req cull requests (view windows of
+    log-uniform 1k-1M objects, 1,000 dynamic rotations each), submitted at the given arrival times
+    (open loop) or whenever fewer than max_outstanding are unfinished (closed loop). A fresh server
+    per run, so its latency statistics are the run's own."""
     lib = abi.load()
     cfg = abi.ServeConfig(2 << 30, 4, 64, 1000, abi.STRIDE_VULKAN)
     server = C.c_void_p()
     abi.check(lib.blz_serve_create(culler.ctx, C.byref(cfg), C.byref(server)), "serve create")
     rng = np.random.default_rng(seed)
-    n_req = int(seconds * rate)
-    gaps = rng.exponential(1.0 / rate, n_req)
-    arrivals = np.cumsum(gaps)
     counts = np.exp(rng.uniform(math.log(1000), math.log(1_000_000), n_req)).astype(np.int64)
     starts = np.array([rng.integers(0, scene.count - c) for c in counts])
     axes = rng.normal(size=(64, 1000, 3))
@@ -180,15 +181,21 @@ def serving(culler, scene, device, seconds=3.0, rate=2000.0, seed=0) -> dict:
     old_switch = sys.getswitchinterval()
     sys.setswitchinterval(2e-5)  # the consumer thread must get the GIL between arrivals
     th.start()
+    late = 0.0  # how far behind its schedule the open-loop submission ran, at most
     t0 = time.perf_counter()
     req = abi.ServeRequest()
     for k in range(n_req):
-        while True:  # sleep through the gap (releasing the GIL), spin only its last 100 us
-            left = arrivals[k] - (time.perf_counter() - t0)
-            if left <= 0:
-                break
-            if left > 150e-6:
-                time.sleep(left - 100e-6)
+        if arrivals is not None:
+            while True:  # sleep through the gap (releasing the GIL), spin only its last 100 us
+                left = arrivals[k] - (time.perf_counter() - t0)
+                if left <= 0:
+                    late = max(late, -left)
+                    break
+                if left > 150e-6:
+                    time.sleep(left - 100e-6)
+        else:
+            while k - len(released) >= max_outstanding:
+                time.sleep(10e-6)
         req.view = views[k % 64]
         req.list = RenderList(objs_dev.data_ptr() + int(starts[k]) * 8, int(counts[k]))
         req.mode = abi.MODE_FRUSTUM
@@ -207,10 +214,39 @@ def serving(culler, scene, device, seconds=3.0, rate=2000.0, seed=0) -> dict:
     st = abi.ServeStats()
     lib.blz_serve_stats(server, C.byref(st))
     lib.blz_serve_destroy(server)
-    return {"requests": n_req, "offered_rate_per_s": rate, "elapsed_s": elapsed, "p50_ms": st.p50Ms,
-            "p99_ms": st.p99Ms, "mean_ms": st.meanMs, "max_ms": st.maxMs, "batches": st.batches,
-            "max_batch": st.maxBatchSize, "max_concurrent_batches": st.maxConcurrentBatches,
-            "objects_per_s": float(counts.sum()) / elapsed, "errors": int(sum(1 for s in released if s))}
+    return {"requests": n_req, "elapsed_s": elapsed, "achieved_rate_per_s": n_req / elapsed,
+            "p50_ms": st.p50Ms, "p99_ms": st.p99Ms, "mean_ms": st.meanMs, "max_ms": st.maxMs,
+            "batches": st.batches, "max_batch": st.maxBatchSize, "max_concurrent_batches": st.maxConcurrentBatches,
+            "objects_per_s": float(counts.sum()) / elapsed, "errors": int(sum(1 for s in released if s)),
+            "submit_late_ms": late * 1e3}
+
+
+def serving(culler, scene, device, seconds=2.0, rates=(2000.0, 8000.0, 20000.0, 50000.0), p99_bound_ms=1.0,
+            seed=0) -> dict:
+    """The serving loop at Poisson arrival rates (open loop, `seconds` each) and closed loop with 64
+    requests outstanding (its saturation throughput). Latency runs from a request's submission to
+    its completion event; `submit_late_ms` says how far the submitting thread fell behind the
+    schedule, so a point whose submissions could not keep up is visible as such.
+    `max_rate_p99_under_bound` is the highest offered rate whose p99 stayed under p99_bound_ms and
+    whose requests were all served at that rate."""
+    curve = []
+    for i, rate in enumerate(rates):
+        rng = np.random.default_rng(seed + 17 * i)
+        n_req = int(seconds * rate)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+        pt = _serve_run(culler, scene, n_req, seed + i, arrivals=arrivals)
+        pt["offered_rate_per_s"] = rate
+        curve.append(pt)
+    closed = _serve_run(culler, scene, 40_000, seed + 99, max_outstanding=64)
+    ok = [p["offered_rate_per_s"] for p in curve
+          if p["p99_ms"] < p99_bound_ms and p["errors"] == 0 and p["achieved_rate_per_s"] >= 0.95 * p["offered_rate_per_s"]]
+    first = curve[0]
+    return {"offered_rate_per_s": first["offered_rate_per_s"], "p50_ms": first["p50_ms"], "p99_ms": first["p99_ms"],
+            "objects_per_s": first["objects_per_s"], "curve": curve, "p99_bound_ms": p99_bound_ms,
+            "max_rate_p99_under_bound": max(ok) if ok else None,
+            "saturation": {"outstanding": 64, "requests_per_s": closed["achieved_rate_per_s"],
+                           "objects_per_s": closed["objects_per_s"], "p50_ms": closed["p50_ms"],
+                           "p99_ms": closed["p99_ms"], "max_batch": closed["max_batch"], "errors": closed["errors"]}}
 
 
 def _replay_ms(culler, fn, reps, flush, stream) -> float:
@@ -259,22 +295,36 @@ def instanced(culler, scene, device, reps=30, slots=100_000) -> dict:
 
 def clusters(device, reps=30) -> dict:
     """The cluster cull over the cluster configuration: 50k objects, 32 meshes of ~200 clusters,
-    frustum + Hi-Z + LOD per object, then sphere frustum + Hi-Z + normal cone per cluster."""
+    frustum + LOD per object, then sphere frustum + Hi-Z + normal cone per cluster.
+
+    The rate reported is cluster tests per second: the clusters actually tested (the chosen LOD's
+    clusters of every object inside the frustum) over the time. That count is measured on the GPU by
+    the same cull over a copy of the scene whose clusters pass every test (radius 1e6, a zero cone
+    axis with cutoff 127, no pyramid), which emits exactly its candidates."""
     from .culler import Culler
     sc = S.cluster_scene(50_000, seed=0)
     c = Culler(device.index if device.index is not None else 0)
     try:
-        c.setup_for_rendering(sc)
         v = abi.view_setup(S.fov_radians(), float(W), float(H), S.ZNEAR, 1e4, (0.0, 0.0, -50.0), 0, 0, W / 2, H / 2)
-        depth = torch.zeros(W * H, dtype=torch.float32, device=device)
-        c.raster_boxes(v, torch.from_numpy(sc.boxes.reshape(-1)).to(device), depth, W, H)
-        pyr = DevicePyramid(W, H, abi.HIZ_D3D12, device)
-        c.generate_depth_pyramid(pyr, depth)
         per_surface = np.array([int(sc.lods[int(s["lodOffset"]):int(s["lodOffset"]) + int(s["lodCount"])]["clusterCount"].max())
                                 for s in sc.surfaces], np.int64)
         cap = int(per_surface[sc.objects["surfaceId"]].sum())
         t = Target.alloc(cap, abi.STRIDE_VULKAN, device)
         ids = torch.empty(cap, dtype=torch.int32, device=device)
+        # the number of clusters tested: the same cull with every cluster test passing
+        opened = S.Scene(sc.objects, sc.transforms, sc.surfaces, sc.lods, clusters=sc.clusters.copy())
+        opened.clusters["radius"] = np.float32(1e6)
+        opened.clusters["coneAxis"] = 0
+        opened.clusters["coneCutoff"] = 127
+        c.setup_for_rendering(opened)
+        c.cluster_cull(v, t)
+        c.check()
+        tested = int(t.read()[0])
+        c.setup_for_rendering(sc)
+        depth = torch.zeros(W * H, dtype=torch.float32, device=device)
+        c.raster_boxes(v, torch.from_numpy(sc.boxes.reshape(-1)).to(device), depth, W, H)
+        pyr = DevicePyramid(W, H, abi.HIZ_D3D12, device)
+        c.generate_depth_pyramid(pyr, depth)
         flush = torch.ones(128 << 20, dtype=torch.int32, device=device)
         side = torch.cuda.Stream(device)
         ms = _replay_ms(c, lambda: c.cluster_cull(v, t, pyramid=pyr, cluster_ids=ids), reps, flush, side)
@@ -287,12 +337,12 @@ def clusters(device, reps=30) -> dict:
         c.check(side)
         nt, npl = (int(x) for x in tt.read()[:2])
         tbytes = sc.count * (8 + 32) + sc.clusters.nbytes + nt * 16 + npl * 132
-        return {"objects": sc.count, "clusters_in_scene": len(sc.clusters), "cluster_upper_bound": cap,
-                "clusters_emitted": n, "ms": ms, "objects_per_s": sc.count / (ms * 1e-3),
-                "cluster_candidates_per_s": cap / (ms * 1e-3), "algorithmic_bytes": nbytes,
-                "GB/s": nbytes / (ms * 1e-3) / 1e9,
+        return {"objects": sc.count, "clusters_in_scene": len(sc.clusters), "clusters_tested": tested,
+                "cluster_capacity_bound": cap, "clusters_emitted": n, "ms": ms,
+                "objects_per_s": sc.count / (ms * 1e-3), "cluster_tests_per_s": tested / (ms * 1e-3),
+                "algorithmic_bytes": nbytes, "GB/s": nbytes / (ms * 1e-3) / 1e9,
                 "task_form": {"ms": ms_t, "tasks": nt, "payloads": npl, "algorithmic_bytes": tbytes,
-                              "cluster_candidates_per_s": cap / (ms_t * 1e-3)}}
+                              "cluster_tests_per_s": tested / (ms_t * 1e-3)}}
     finally:
         c.close()
 

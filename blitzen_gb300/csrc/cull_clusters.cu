@@ -27,10 +27,11 @@ constexpr int kClWarps = kClThreads / 32;
 constexpr uint32_t kClObjects = 32;  // objects per tile
 constexpr uint32_t kClMaxSplit = 4;  // test blocks per tile, at most
 
-// Sphere, Hi-Z and cone tests of one cluster of an object. snorm[i] holds (float)(i - 128) / 127,
-// divided once per block: the int8 cone axis and cutoff take only those 256 values.
+// Sphere, Hi-Z and cone tests of one cluster of an object. The int8 cone axis and cutoff are divided
+// by 127 only for the clusters that reach the cone test (about 2 % of them behind the occluders of a
+// typical frame), not per block for every value they can take.
 __device__ __forceinline__ bool cluster_visible(const ClusterParams& p, const ViewConsts& v, const float4 posScale,
-                                                const float4 quat, uint32_t cid, const float* snorm) {
+                                                const float4 quat, uint32_t cid) {
     const float4* cp = reinterpret_cast<const float4*>(p.sc.clusters + cid);
     const float4 sph = __ldg(cp);
     const uint32_t cone = __ldg(reinterpret_cast<const uint32_t*>(cp + 1));  // int8 axis xyz, cutoff
@@ -45,8 +46,9 @@ __device__ __forceinline__ bool cluster_visible(const ClusterParams& p, const Vi
     if (vis) {
         const int ax = static_cast<int8_t>(cone & 0xFFu), ay = static_cast<int8_t>((cone >> 8) & 0xFFu);
         const int az = static_cast<int8_t>((cone >> 16) & 0xFFu), ac = static_cast<int8_t>(cone >> 24);
-        const Vec3 axm{snorm[ax + 128], snorm[ay + 128], snorm[az + 128]};
-        const float cutoff = snorm[ac + 128];
+        const Vec3 axm{BLZ_FD(static_cast<float>(ax), 127.0f), BLZ_FD(static_cast<float>(ay), 127.0f),
+                       BLZ_FD(static_cast<float>(az), 127.0f)};
+        const float cutoff = BLZ_FD(static_cast<float>(ac), 127.0f);
         const Vec3 axis = rotate_quat(axm, quat);
         const float dx = BLZ_FS(w.x, v.camX), dy = BLZ_FS(w.y, v.camY), dz = BLZ_FS(w.z, v.camZ);
         const float len = __fsqrt_rn(BLZ_FA(BLZ_FA(BLZ_FM(dx, dx), BLZ_FM(dy, dy)), BLZ_FM(dz, dz)));
@@ -227,13 +229,10 @@ __global__ void __launch_bounds__(kClThreads) cluster_test_kernel(const ClusterP
     __shared__ uint32_t s_start[kClObjects + 1];
     __shared__ uint32_t s_warp[kClWarps];
     __shared__ uint32_t s_surv[kClObjects];
-    __shared__ float s_snorm[256];
     const uint32_t tile = blockIdx.x / p.split, part = blockIdx.x - tile * p.split;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t T = __ldcg(p.tileSlots + tile);
     if (part * static_cast<uint32_t>(kClThreads) >= T) return;  // no chunk for this block
-    for (uint32_t i = threadIdx.x; i < 256u; i += kClThreads)
-        s_snorm[i] = BLZ_FD(static_cast<float>(static_cast<int>(i) - 128), 127.0f);
     if (warp == 0) {
         const uint32_t o = tile * kClObjects + lane;
         const uint2 info = __ldcg(p.objInfo + o);
@@ -260,7 +259,7 @@ __global__ void __launch_bounds__(kClThreads) cluster_test_kernel(const ClusterP
         uint32_t lo = 0;
         if (slot < T) {
             lo = slot_object(s_start, slot);
-            vis = cluster_visible(p, v, s_xf[lo][0], s_xf[lo][1], s_off[lo] + (slot - s_start[lo]), s_snorm);
+            vis = cluster_visible(p, v, s_xf[lo][0], s_xf[lo][1], s_off[lo] + (slot - s_start[lo]));
         }
         uint32_t bal = __ballot_sync(0xFFFFFFFFu, vis);
         if (lane == 0 && bal != 0u) {
