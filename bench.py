@@ -15,6 +15,9 @@ value  = objects per second of the device-timed frames: each step replays blz_cu
          blz_pyramid_build + blz_cull_late) are timed the same way in `frame_forms`, and every part
          as its own graph in `roofline.others`. All three forms give the same records, counts,
          pyramid and visibility, checked against the oracle (`bit_exact`).
+roofline = the headline frame's sweep (blz_cull_frame over the pyramid already built: the decide
+         launch for both passes and the launch writing both record lists), algorithmic bytes over
+         its CUDA-event time, against the measured copy bandwidth.
 e2e    = the same frame through the C ABI with host buffers, all inside the timed region: the host
          writes the 1,000 dynamic transform rows into a pinned buffer and replays the recorded step
          (blz_graph_launch): the 8.3 MB depth upload and the pyramid run beside blz_frame_first,
@@ -228,16 +231,17 @@ def frame_matches(want, t1, t2, vis, pyr) -> bool:
     return bool(ok)
 
 
-def recorded_traffic(kernel: str, objects: int):
-    """DRAM bytes per launch of `kernel` on the stress frame from the committed ncu figures, or None."""
+def recorded_traffic(kernels, objects: int):
+    """DRAM bytes of one launch of each of `kernels`, summed, on the stress frame from the committed
+    ncu figures, or None when a kernel is missing or was captured on another scene size."""
     try:
         with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
             d = json.load(f)
-        e = d["kernels"][kernel]
-        if int(e["objects"]) != objects:
+        es = [d["kernels"][k] for k in kernels]
+        if any(int(e["objects"]) != objects for e in es):
             return None
-        return {"bytes_per_launch": int(e["dram_bytes_per_launch"]),
-                "source": f"ncu capture at commit {d['commit']}: {e['command']}"}
+        return {"bytes_per_launch": sum(int(e["dram_bytes_per_launch"]) for e in es),
+                "source": f"ncu capture at commit {d['commit']}: {d['command']}"}
     except Exception:
         return None
 
@@ -343,7 +347,8 @@ def main():
         kernels_per_step = graphs["one_call"].kernels
         # each part on its own, for the breakdown (frame_late reuses what the last pass 1 kept)
         parts = {}
-        for name, fn in (("frame_first", lambda: c.frame_first_pass(v, vis, t1)),
+        for name, fn in (("sweep", lambda: c.cull_frame(v, vis, None, pyr, t1, t2)),
+                         ("frame_first", lambda: c.frame_first_pass(v, vis, t1)),
                          ("pyramid", lambda: c.generate_depth_pyramid(pyr, depth)),
                          ("frame_late", lambda: c.frame_occlusion_pass(pyr, t2)),
                          ("pass1", lambda: c.draw_cull_first_pass(v, vis, t1)),
@@ -374,6 +379,11 @@ def main():
         exact["timed_frame"] = frame_matches(want, t1, t2, vis, pyr)
         t_form = {name: statistics.mean(timed(g, args.steps)) for name, g in graphs.items()}
         t_part = {name: statistics.mean(timed(g, args.steps)) for name, g in parts.items()}
+        # the sweep over the pyramid the replays left: the same frame as the headline's
+        vis.copy_(vis0)
+        parts["sweep"].launch()
+        side.synchronize()
+        exact["sweep"] = frame_matches(want, t1, t2, vis, pyr)
         t_ab = statistics.mean(timed(frame_ab, args.steps))
     c.check()
     t_step = max_over_ranks(sum(ms) / len(ms), world, dev)
@@ -381,33 +391,43 @@ def main():
         dist.barrier()
     value = job_throughput(N, world, t_step)
 
-    # roofline: the dominant kernel of the frame is the kept frame's pass 1 (every object's render
-    # object, transform and visibility read once); algorithmic bytes per launch are the bytes the
-    # reference's passes must move for it: render object + transform + visibility word per object,
-    # the visibility words it settles (candidates outside the frustum) and pass 1's records
+    # roofline: the dominant work of the headline frame is its sweep, the two launches after the
+    # pyramid (cull_decide_kernel<5> deciding both passes for every object, cull_scatter2_kernel
+    # writing both record lists), timed as blz_cull_frame over the pyramid already built. Its
+    # algorithmic bytes are what the reference's two passes must move: each object's render object
+    # and transform read once, its visibility word read once and rewritten (pass 2 writes every
+    # object's), both record lists and their counts
     stride = abi.STRIDE_VULKAN
     mip_bytes = pyr.storage.numel() * 4
     bytes_pyr = W * H * 4 + mip_bytes
+    bytes_sweep = N * (8 + 32) + 4 * N + 4 * N + (V1 + V2) * stride + 8
     bytes_a = N * (8 + 32 + 4) + 4 * (n_prev - V1) + V1 * stride + 4
-    bytes_frame = N * (8 + 32) + 4 * N + 4 * N + (V1 + V2) * stride + 8 + bytes_pyr
+    bytes_frame = bytes_sweep + bytes_pyr
     bytes_late = N * (8 + 32) + 4 * N + 4 * N + V2 * stride + 4
     bytes_first = 4 * N + n_prev * (8 + 32) + V1 * stride + 4
     peak, peak_kind = peaks()
-    t_a = t_part["frame_first"]
-    ach = bytes_a / (t_a * 1e-3) / 1e9
+    t_sw = t_part["sweep"]
+    ach = bytes_sweep / (t_sw * 1e-3) / 1e9
 
     def gbs(b, t):
         return b / (t * 1e-3) / 1e9
 
-    roofline = {"bound": "hbm", "kernel": "kept-frame pass 1: cull_decide_kernel<4> + cull_scatter_kernel",
+    roofline = {"bound": "hbm", "kernel": "one-call frame sweep: cull_decide_kernel<5> + cull_scatter2_kernel",
                 "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
-                "traffic": None, "algorithmic_bytes": bytes_a, "ms": t_a,
-                "ms_note": "the kept frame's pass 1 (blz_frame_first) recorded as its own graph",
+                "traffic": None, "algorithmic_bytes": bytes_sweep, "ms": t_sw,
+                "ms_note": "blz_cull_frame with no depth (the pyramid already built) recorded as its own graph: "
+                           "the headline frame minus its pyramid launch",
                 "others": {
                     "frame": {"ms": t_step, "bytes": bytes_frame, "GB/s": gbs(bytes_frame, t_step),
                               "frac": gbs(bytes_frame, t_step) / peak,
                               "note": "blz_cull_frame; bytes: every object's tables and visibility read once, "
                                       "visibility written once, both record lists, the pyramid"},
+                    "frame_first": {"ms": t_part["frame_first"], "bytes": bytes_a,
+                                    "GB/s": gbs(bytes_a, t_part["frame_first"]),
+                                    "frac": gbs(bytes_a, t_part["frame_first"]) / peak,
+                                    "note": "kept frame's pass 1 (cull_decide_kernel<4> + cull_scatter_kernel); "
+                                            "bytes: tables + visibility read, the visibility words it settles, "
+                                            "pass 1's records"},
                     "frame_late": {"ms": t_part["frame_late"], "note": "survivors' pyramid test + scatter"},
                     "pyramid": {"ms": t_part["pyramid"], "bytes": bytes_pyr, "GB/s": gbs(bytes_pyr, t_part["pyramid"])},
                     "pass1": {"ms": t_part["pass1"], "bytes": bytes_first, "GB/s": gbs(bytes_first, t_part["pass1"])},
@@ -417,7 +437,7 @@ def main():
     frames = {name: {"ms": t, "objects_per_s": job_throughput(N, world, t)} for name, t in t_form.items()}
     # DRAM bytes per launch from an ncu capture (profiles/dram_traffic.json names the commit and the
     # command it was taken with); a capture, not a measurement of this run
-    traffic = recorded_traffic("cull_decide_kernel<4>", args.objects)
+    traffic = recorded_traffic(("cull_decide_kernel<5>", "cull_scatter2_kernel"), args.objects)
     if traffic:
         roofline["traffic"] = traffic["bytes_per_launch"]
         roofline["traffic_source"] = traffic["source"]

@@ -740,12 +740,15 @@ int blz_cull_frame(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list
     if (rc != BLZ_OK) return rc;
     rc = check_pyramid(pyr, true);
     if (rc != BLZ_OK) return rc;
-    if (!depth) return fail(BLZ_ERR_INVALID_ARGUMENT, "depth is NULL");
-    if (pyr->depthWidth == 0 || pyr->depthHeight == 0) return fail(BLZ_ERR_INVALID_ARGUMENT, "pyramid has no depth extent");
+    if (depth && (pyr->depthWidth == 0 || pyr->depthHeight == 0))
+        return fail(BLZ_ERR_INVALID_ARGUMENT, "pyramid has no depth extent");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    // the pyramid, then one sweep deciding both passes, then both record lists in one launch
-    rc = blz_pyramid_build(c, pyr, depth, stream);
-    if (rc != BLZ_OK) return rc;
+    // the pyramid (unless the caller built it), then one sweep deciding both passes, then both
+    // record lists in one launch
+    if (depth) {
+        rc = blz_pyramid_build(c, pyr, depth, stream);
+        if (rc != BLZ_OK) return rc;
+    }
     PipeParams p2 = p1;  // pass 2's records: staged / chunkCount, target 2
     p2.single.mode = BLZ_MODE_LATE;
     p2.single.pyr = pyramid_view(pyr);

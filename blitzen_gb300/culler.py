@@ -251,13 +251,14 @@ class Culler:
         check(self.lib.blz_frame_late(self.ctx, C.byref(pyramid.desc), C.byref(t), _stream_ptr(stream)),
               "blz_frame_late")
 
-    def cull_frame(self, view, visibility: torch.Tensor, depth: torch.Tensor, pyramid: DevicePyramid, target1: Target,
-                   target2: Target, objects=None, count=None, stream=None):
-        """Both occlusion passes and the pyramid of one frame in one call (blz_cull_frame)."""
+    def cull_frame(self, view, visibility: torch.Tensor, depth: torch.Tensor | None, pyramid: DevicePyramid,
+                   target1: Target, target2: Target, objects=None, count=None, stream=None):
+        """Both occlusion passes and the pyramid of one frame in one call (blz_cull_frame). depth None
+        uses the pyramid as it stands instead of building it."""
         a, b = target1.ctype(), target2.ctype()
         check(self.lib.blz_cull_frame(self.ctx, C.byref(view), self._list(objects, count), visibility.data_ptr(),
-                                      depth.data_ptr(), C.byref(pyramid.desc), C.byref(a), C.byref(b),
-                                      _stream_ptr(stream)), "blz_cull_frame")
+                                      depth.data_ptr() if depth is not None else None, C.byref(pyramid.desc),
+                                      C.byref(a), C.byref(b), _stream_ptr(stream)), "blz_cull_frame")
 
     def draw_cull_temporal(self, view, pyramid: DevicePyramid, target: Target, objects=None, count=None, stream=None):
         t = target.ctype()

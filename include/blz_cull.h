@@ -283,8 +283,9 @@ int blz_frame_late(blz_ctx* ctx, const BlzPyramid* pyramid, const BlzCullTarget*
  * frame, inside the frustum, not occluded) or neither, rewriting the visibility as pass 2 does; one
  * final launch writes both record lists. Same records, counts, pyramid and visibility as
  * blz_cull_first + blz_pyramid_build + blz_cull_late on the same inputs. It keeps nothing for
- * blz_frame_late. Replaces the pass order of VulkanRenderer::DrawFrame (vulkanDraw.cpp:1015-1031)
- * and dx12Draw.cpp:590-641 minus the draws. */
+ * blz_frame_late. dDepth NULL: the pyramid is used as it stands (a caller that built it itself,
+ * with blz_pyramid_build earlier or from another frame's depth). Replaces the pass order of
+ * VulkanRenderer::DrawFrame (vulkanDraw.cpp:1015-1031) and dx12Draw.cpp:590-641 minus the draws. */
 int blz_cull_frame(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list, uint32_t* dVisibility,
                    const float* dDepth, const BlzPyramid* pyramid, const BlzCullTarget* pass1Target,
                    const BlzCullTarget* pass2Target, blz_stream_t stream);

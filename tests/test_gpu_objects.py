@@ -153,7 +153,8 @@ def test_pyramid_odd_sizes(sculler, wh, mode):
 def run_frame(c, form, v, vis, depth, pyr, t1, t2, objects=None, count=None):
     """One occlusion frame in one of the library's three forms: the separate calls (blz_cull_first,
     blz_pyramid_build, blz_cull_late), the kept frame (blz_frame_first, blz_pyramid_build,
-    blz_frame_late) or the one call (blz_cull_frame)."""
+    blz_frame_late), the one call (blz_cull_frame) or the one call over a pyramid built before it
+    (blz_cull_frame with no depth)."""
     if form == "calls":
         c.draw_cull_first_pass(v, vis, t1, objects=objects, count=count)
         c.generate_depth_pyramid(pyr, depth)
@@ -162,11 +163,14 @@ def run_frame(c, form, v, vis, depth, pyr, t1, t2, objects=None, count=None):
         c.frame_first_pass(v, vis, t1, objects=objects, count=count)
         c.generate_depth_pyramid(pyr, depth)
         c.frame_occlusion_pass(pyr, t2)
+    elif form == "prebuilt":
+        c.generate_depth_pyramid(pyr, depth)
+        c.cull_frame(v, vis, None, pyr, t1, t2, objects=objects, count=count)
     else:
         c.cull_frame(v, vis, depth, pyr, t1, t2, objects=objects, count=count)
 
 
-FORMS = ["calls", "kept", "one_call"]
+FORMS = ["calls", "kept", "one_call", "prebuilt"]
 
 
 @pytest.mark.parametrize("form", FORMS)
