@@ -166,6 +166,7 @@ _PROTOS = {
     "blz_ctx_check": (_I, [_P, _P, C.POINTER(_U32)]),
     "blz_ctx_set_wait_limit": (_I, [_P, _U32]),
     "blz_ctx_debug_advance_ticket": (_I, [_P, _U32, _P]),
+    "blz_ctx_debug_skip_frame_tiles": (_I, [_P, _U32, _P]),
     "blz_ctx_launch_count": (C.c_uint64, [_P]),
     "blz_scene_upload": (_I, [_P, C.POINTER(SceneDesc), _U32, _P]),
     "blz_scene_device_tables": (_I, [_P, C.POINTER(SceneDesc)]),

@@ -250,6 +250,14 @@ int blz_ctx_debug_advance_ticket(blz_ctx* c, uint32_t n, blz_stream_t stream) {
     return BLZ_OK;
 }
 
+int blz_ctx_debug_skip_frame_tiles(blz_ctx* c, uint32_t n, blz_stream_t stream) {
+    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (n == 0 || n > 1024) return fail(BLZ_ERR_INVALID_ARGUMENT, "tile skip %u outside [1, 1024]", n);
+    cudaError_t e = launch_add_word(&c->scratch->frameTicket, n, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "frame ticket advance");
+    return BLZ_OK;
+}
+
 int blz_ctx_check(blz_ctx* c, blz_stream_t stream, uint32_t* flagsOut) {
     if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -473,13 +481,16 @@ uint64_t blz_pyramid_layout(uint32_t dw, uint32_t dh, uint32_t mode, BlzPyramid*
     return at * sizeof(float);
 }
 
-int blz_pyramid_build(blz_ctx* c, const BlzPyramid* p, const float* depth, blz_stream_t stream) {
-    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+namespace blz {
+
+// The parameters of one pyramid build from `depth` (checked), for the pyramid kernel or the
+// one-call frame kernel.
+static int pyramid_build_params(blz_ctx* c, const BlzPyramid* p, const float* depth, PyramidBuildParams& bp) {
     int rc = check_pyramid(p, true);
     if (rc != BLZ_OK) return rc;
     if (!depth) return fail(BLZ_ERR_INVALID_ARGUMENT, "depth is NULL");
     if (p->depthWidth == 0 || p->depthHeight == 0) return fail(BLZ_ERR_INVALID_ARGUMENT, "pyramid has no depth extent");
-    PyramidBuildParams bp{};
+    bp = PyramidBuildParams{};
     bp.depth = depth;
     bp.depthWidth = p->depthWidth;
     bp.depthHeight = p->depthHeight;
@@ -493,6 +504,17 @@ int blz_pyramid_build(blz_ctx* c, const BlzPyramid* p, const float* depth, blz_s
     bp.vec4 = (p->mode == BLZ_HIZ_D3D12 && p->depthWidth % 4 == 0 && p->depthHeight >= 2 &&
                p->width == p->depthWidth / 2 && p->height <= p->depthHeight / 2 && p->mipOffset[0] == 0 &&
                reinterpret_cast<uintptr_t>(depth) % 16 == 0 && reinterpret_cast<uintptr_t>(p->data) % 8 == 0) ? 1u : 0u;
+    bp.spinLimit = c->waitLimit ? c->waitLimit : kSpinLimitDefault;
+    return BLZ_OK;
+}
+
+}  // namespace blz
+
+int blz_pyramid_build(blz_ctx* c, const BlzPyramid* p, const float* depth, blz_stream_t stream) {
+    if (!c) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    PyramidBuildParams bp;
+    int rc = pyramid_build_params(c, p, depth, bp);
+    if (rc != BLZ_OK) return rc;
     uint32_t launches = 0;
     cudaError_t e = launch_pyramid_build(bp, reinterpret_cast<cudaStream_t>(stream), &launches);
     if (e != cudaSuccess) return cuda_fail(e, "pyramid launch");
@@ -740,15 +762,12 @@ int blz_cull_frame(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list
     if (rc != BLZ_OK) return rc;
     rc = check_pyramid(pyr, true);
     if (rc != BLZ_OK) return rc;
-    if (depth && (pyr->depthWidth == 0 || pyr->depthHeight == 0))
-        return fail(BLZ_ERR_INVALID_ARGUMENT, "pyramid has no depth extent");
-    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    // the pyramid (unless the caller built it), then one sweep deciding both passes, then both
-    // record lists in one launch
+    PyramidBuildParams bp;
     if (depth) {
-        rc = blz_pyramid_build(c, pyr, depth, stream);
+        rc = pyramid_build_params(c, pyr, depth, bp);
         if (rc != BLZ_OK) return rc;
     }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     PipeParams p2 = p1;  // pass 2's records: staged / chunkCount, target 2
     p2.single.mode = BLZ_MODE_LATE;
     p2.single.pyr = pyramid_view(pyr);
@@ -757,13 +776,16 @@ int blz_cull_frame(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list
     set_target(p2, target2);
     p2.staged2 = fb.staged2;  // pass 1's records
     p2.chunkCount2 = fb.count2;
-    cudaError_t e = launch_frame_fused(p2, c->singleThreads, c->singleOpt, c->smCount, st);
+    // one launch building the pyramid's tiles and then deciding both passes in one sweep (or the
+    // sweep alone over the pyramid the caller built), then both record lists in one launch
+    cudaError_t e = depth ? launch_frame_pyr(p2, bp, c->singleThreads, c->singleOpt, c->smCount, st)
+                          : launch_frame_fused(p2, c->singleThreads, c->singleOpt, c->smCount, st);
     PipeParams q1 = p1;  // pass 1's list for the scatter
     q1.staged = fb.staged2;
     q1.chunkCount = fb.count2;
     if (e == cudaSuccess) e = launch_frame_scatter2(q1, p2, st);
     if (e != cudaSuccess) return cuda_fail(e, "frame launch");
-    c->launches += 2;  // the sweep + both scatters
+    c->launches += 2;  // the sweep (with the pyramid) + both scatters
     c->frameOpen = false;  // the fused sweep keeps no survivors for blz_frame_late
     return BLZ_OK;
 }

@@ -178,14 +178,23 @@ __device__ __forceinline__ uint32_t mip_dim(uint32_t base, uint32_t level) {
     return d ? d : 1u;
 }
 
+// A pyramid texel load. COH: the pyramid was written during this launch (the one-call frame
+// kernel builds it), so the load goes to L2 (coherent), not through the read-only path.
+template <bool COH>
+__device__ __forceinline__ float pyr_ld(const float* a) {
+    return COH ? __ldcg(a) : __ldg(a);
+}
+
+template <bool COH = false>
 __device__ __forceinline__ float pyr_load(const PyramidView& p, uint32_t level, uint32_t x, uint32_t y) {
     if (level >= p.mipCount) return 0.0f;
     uint32_t w = mip_dim(p.width, level), h = mip_dim(p.height, level);
     if (x >= w || y >= h) return 0.0f;
-    return __ldg(p.data + p.mipOffset[level] + static_cast<size_t>(y) * w + x);
+    return pyr_ld<COH>(p.data + p.mipOffset[level] + static_cast<size_t>(y) * w + x);
 }
 
 // hlslMath.hlsl:58-78 (OcclusionCheck): one-texel Load at mip floor(log2(max extent)).
+template <bool COH = false>
 __device__ __forceinline__ bool occlusion_d3d12(float4 a, const PyramidView& p, const ViewConsts& v, Vec3 c, float r) {
     uint32_t pw = ftou(v.pyramidWidth), ph = ftou(v.pyramidHeight);
     float width = BLZ_FM(BLZ_FS(a.z, a.x), static_cast<float>(pw));
@@ -198,7 +207,7 @@ __device__ __forceinline__ bool occlusion_d3d12(float4 a, const PyramidView& p, 
         mh = mh ? mh : 1u;
         float sw = BLZ_FM(static_cast<float>(mw), 0.5f), sh = BLZ_FM(static_cast<float>(mh), 0.5f);
         float ax = BLZ_FM(a.x, sw), ay = BLZ_FM(a.y, sh), az = BLZ_FM(a.z, sw), aw = BLZ_FM(a.w, sh);
-        depth = pyr_load(p, level, ftou(BLZ_FA(ax, az)), ftou(BLZ_FA(ay, aw)));
+        depth = pyr_load<COH>(p, level, ftou(BLZ_FA(ax, az)), ftou(BLZ_FA(ay, aw)));
     }
     float depthSphere = BLZ_FD(v.zNear, BLZ_FS(c.z, r));
     return depthSphere > depth;
@@ -213,6 +222,7 @@ __device__ __forceinline__ long long to_index(float f) {
 }
 
 // MIN-reduction bilinear footprint (LINEAR + MIN sampler, clamp to edge) at (s, t) of one mip.
+template <bool COH = false>
 __device__ __forceinline__ float min_footprint(const float* img, uint32_t w, uint32_t h, float s, float t) {
     float u = BLZ_FS(BLZ_FM(s, static_cast<float>(w)), 0.5f);
     float vv = BLZ_FS(BLZ_FM(t, static_cast<float>(h)), 0.5f);
@@ -230,13 +240,14 @@ __device__ __forceinline__ float min_footprint(const float* img, uint32_t w, uin
             long long x = xs[ix], y = ys[jy];
             x = x < 0 ? 0 : (x > (long long)w - 1 ? (long long)w - 1 : x);
             y = y < 0 ? 0 : (y > (long long)h - 1 ? (long long)h - 1 : y);
-            m = fmin_nan(m, __ldg(img + static_cast<size_t>(y) * w + static_cast<size_t>(x)));
+            m = fmin_nan(m, pyr_ld<COH>(img + static_cast<size_t>(y) * w + static_cast<size_t>(x)));
         }
     return m;
 }
 
 // CullingShaderData.glsl:60-73 (OcclusionCullingPassed) with the MIN sampler of
 // vulkanResources.cpp:51-55 (NEAREST mip, LOD clamped to [0, 16] and to the last mip).
+template <bool COH = false>
 __device__ __forceinline__ bool occlusion_vulkan(float4 a, const PyramidView& p, const ViewConsts& v, Vec3 c, float r) {
     float width = BLZ_FM(BLZ_FS(a.z, a.x), v.pyramidWidth);
     float height = BLZ_FM(BLZ_FS(a.w, a.y), v.pyramidHeight);
@@ -248,13 +259,14 @@ __device__ __forceinline__ bool occlusion_vulkan(float4 a, const PyramidView& p,
     if (d > p.mipCount - 1u) d = p.mipCount - 1u;
     uint32_t w = mip_dim(p.width, d), h = mip_dim(p.height, d);
     float s = BLZ_FM(BLZ_FA(a.x, a.z), 0.5f), t = BLZ_FM(BLZ_FA(a.y, a.w), 0.5f);
-    float depth = min_footprint(p.data + p.mipOffset[d], w, h, s, t);
+    float depth = min_footprint<COH>(p.data + p.mipOffset[d], w, h, s, t);
     float depthSphere = BLZ_FD(v.zNear, BLZ_FS(c.z, r));
     return depthSphere > depth;
 }
 
+template <bool COH = false>
 __device__ __forceinline__ bool occlusion(float4 a, const PyramidView& p, const ViewConsts& v, Vec3 c, float r) {
-    return (p.mode == BLZ_HIZ_VULKAN) ? occlusion_vulkan(a, p, v, c, r) : occlusion_d3d12(a, p, v, c, r);
+    return (p.mode == BLZ_HIZ_VULKAN) ? occlusion_vulkan<COH>(a, p, v, c, r) : occlusion_d3d12<COH>(a, p, v, c, r);
 }
 
 // Distance-to-surface threshold for LOD selection; CullingShaderData.glsl:105-106,
@@ -287,7 +299,10 @@ struct Scratch {
     unsigned int doneBlocks;
     unsigned int pyrDone;        // pyramid build: tiles finished (zero between builds)
     unsigned int status;         // BLZ_FLAG_* bits
-    unsigned int pad1[27];       // keep the state array on its own 128-byte lines
+    unsigned int frameTicket;    // one-call frame: next pyramid tile to hand out (zero between frames)
+    unsigned int frameTilesDone; // one-call frame: pyramid tiles finished (zero between frames)
+    unsigned int frameReady;     // one-call frame: 1 once the pyramid is complete (zero between frames)
+    unsigned int pad1[24];       // keep the state array on its own 128-byte lines
     unsigned long long state[1]; // [maxTiles] tile states: epoch << 32 | flag << 30 | value
 };
 
@@ -335,6 +350,22 @@ __device__ __forceinline__ void load_transform(const SceneTables& sc, uint32_t t
 // next kernel on the stream be scheduled now, to wait in its own pdl_wait().
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_launch_next() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+__device__ __forceinline__ void st_release_gpu(unsigned int* p, unsigned int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned int atom_add_acq_rel_gpu(unsigned int* p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;

@@ -18,6 +18,7 @@
 //   LATE      LateDrawCull.comp.glsl:13-72,        drawOccLate.cs.hlsl:13-67
 //   TEMPORAL  drawOccTemporal.hlsl:13-64
 #include "blz_device.cuh"
+#include "pyramid_tile.cuh"
 #include "kernels.h"
 
 namespace blz {
@@ -76,17 +77,34 @@ struct Survivor {
 };
 constexpr uint32_t kRing = 64;  // per-warp survivor ring: under 32 waiting plus one 32-object slice
 
+// Both passes of a frame decided in one sweep, with the pyramid built before the launch or inside it.
+__host__ __device__ constexpr bool fused_mode(int m) { return m == kModeFrameFused || m == kModeFramePyr; }
+
+// A warp's wait for the pyramid its own launch builds (kModeFramePyr): the whole warp polls the
+// ready flag with acquire semantics (one load serves every lane, so all see the same value), at
+// most `limit` times; then it raises BLZ_FLAG_TIMEOUT and goes on with whatever the pyramid holds.
+__device__ __forceinline__ void wait_pyramid(const unsigned int* ready, uint32_t limit, unsigned int& flags) {
+    for (uint32_t polls = 0; ld_acquire_gpu(ready) == 0u;) {
+        if (++polls >= limit) {
+            flags |= BLZ_FLAG_TIMEOUT;
+            break;
+        }
+        __nanosleep(128);
+    }
+    __syncwarp();
+}
+
 // Dense stage over one survivor per lane (lanes with `mine`), in object order: the sphere
 // projection and Hi-Z test (LATE/TEMPORAL), LATE's visibility write, LOD selection of the emitted
 // ones, and their staging as (objectId, lodId) after the `run` already staged for the chunk.
 // A survivor is the two words of a Survivor: a = {obj | tags, centre}, b = {r, scale, lodOff, lodCnt}.
 // kModeFrame1 emits the survivors visible last frame (its pass-1 records) and tests no pyramid.
-// kModeFrameFused stages pass 2's records in `stage` and pass 1's in `stage1` (run1).
+// The fused modes stage pass 2's records in `stage` and pass 1's in `stage1` (run1).
 template <int MODE>
 __device__ __forceinline__ void dense_entry(const SceneTables& sc, const BatchViewDev& bv, const ViewConsts& v, uint4 a,
                                             uint4 b, bool mine, uint2* stage, uint32_t& run, uint2* stage1 = nullptr,
                                             uint32_t* run1 = nullptr) {
-    constexpr bool FUSED = MODE == kModeFrameFused;
+    constexpr bool FUSED = fused_mode(MODE);
     constexpr bool REWRITE = MODE == BLZ_MODE_LATE || FUSED;  // pass 2's visibility rewrite
     const uint32_t obj = a.x & 0x3FFFFFFFu;  // LATE: bit 31 previous visibility != 0, bit 30 == 1
     const Vec3 c{__uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(a.w)};
@@ -96,7 +114,8 @@ __device__ __forceinline__ void dense_entry(const SceneTables& sc, const BatchVi
     if (mine) {
         if (MODE == BLZ_MODE_LATE || MODE == BLZ_MODE_TEMPORAL || FUSED) {
             float4 aabb;
-            if (project_sphere(c, r, v.zNear, v.proj0, v.proj5, aabb)) visible = occlusion(aabb, bv.pyr, v, c, r);
+            if (project_sphere(c, r, v.zNear, v.proj0, v.proj5, aabb))
+                visible = occlusion<MODE == kModeFramePyr>(aabb, bv.pyr, v, c, r);
         }
         if (REWRITE) {
             // drawOccLate.cs.hlsl:67, storing only a value that changes
@@ -173,7 +192,8 @@ template <int MODE, bool SINGLE, int OPT>
 __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const BatchViewDev& bv, uint32_t base,
                                                     uint32_t limit, uint2* stage, Survivor* ring, uint4* cand,
                                                     const SurfaceCache& surf, unsigned int& flags, uint4* keep,
-                                                    uint32_t& kept, uint2* stage1 = nullptr, uint32_t* run1 = nullptr) {
+                                                    uint32_t& kept, uint2* stage1 = nullptr, uint32_t* run1 = nullptr,
+                                                    const unsigned int* ready = nullptr, uint32_t spinLimit = 0u) {
     constexpr uint32_t STEP = 32u * OPT;
     constexpr bool PACK = (MODE == BLZ_MODE_FIRST) && SINGLE;  // candidate ring of 2 * STEP entries
     // Single-view pass 2 walks its chunk from the last object down: pass 1 walked the same chunk
@@ -190,12 +210,21 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
         for (uint32_t i = base + lane; i < limit; i += 32u) {
             const bool act = MODE != BLZ_MODE_FIRST || __ldg(bv.vis + i) != 0u;
             if (act) flags |= BLZ_FLAG_BAD_INDEX;
-            if (MODE == BLZ_MODE_LATE || MODE == kModeFrame1 || MODE == kModeFrameFused) bv.vis[i] = 0u;
+            if (MODE == BLZ_MODE_LATE || MODE == kModeFrame1 || fused_mode(MODE)) bv.vis[i] = 0u;
         }
         return 0u;
     }
     const ViewConsts v = load_view(bv.view);
     uint32_t run = 0, head = 0, tail = 0;
+    // kModeFramePyr: the pyramid is waited for once, before the warp's first dense round
+    bool pyrSeen = MODE != kModeFramePyr;
+    auto dense = [&](uint32_t n) {
+        if (!pyrSeen) {
+            wait_pyramid(ready, spinLimit, flags);
+            pyrSeen = true;
+        }
+        dense_round<MODE>(sc, bv, v, ring, head, n, stage, run, keep, kept, stage1, run1);
+    };
 
     // frustum stage over OPT slices: obj[k] the object index, ro[k] its render object, vis[k] the
     // object's visibility word (LATE: as read; the object is active when in range) or, in the other
@@ -205,7 +234,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
     bool ok[OPT];
     // LATE and kModeFrame1 test every object (vis[k] holds its visibility word), the others the
     // objects with vis[k] != 0
-    constexpr bool ALL = MODE == BLZ_MODE_LATE || MODE == kModeFrame1 || MODE == kModeFrameFused;
+    constexpr bool ALL = MODE == BLZ_MODE_LATE || MODE == kModeFrame1 || fused_mode(MODE);
     auto active = [&](uint32_t obj, uint32_t vis) -> bool { return ALL ? obj < limit : vis != 0u; };
     auto gather = [&](const uint32_t (&obj)[OPT], const uint2 (&ro)[OPT], const uint32_t (&vis)[OPT]) {
 #pragma unroll
@@ -254,7 +283,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
             tail += __popc(m);
             if (tail - head >= 32u) {
                 __syncwarp();
-                dense_round<MODE>(sc, bv, v, ring, head, 32u, stage, run, keep, kept, stage1, run1);
+                dense(32u);
                 head += 32u;
                 __syncwarp();
             }
@@ -326,7 +355,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
     }
     if (tail != head) {
         __syncwarp();
-        dense_round<MODE>(sc, bv, v, ring, head, tail - head, stage, run, keep, kept, stage1, run1);
+        dense(tail - head);
         __syncwarp();
     }
     return run;
@@ -350,28 +379,40 @@ __device__ __forceinline__ void put_record(uint8_t* cmds, uint32_t stride, uint3
 
 // ------------------------------------------------------------------ decide kernel
 
+// Shared memory of the decide kernels: one survivor ring per warp, pass 1's candidate rings, and the
+// surface table in what static shared memory is left (48 KB per block).
 template <int MODE, bool SINGLE, int THREADS, int OPT>
-__global__ void __launch_bounds__(THREADS, (SINGLE || MODE >= 0) ? 1024 / THREADS : 1) cull_decide_kernel(const PipeParams p) {
-    constexpr int NW = THREADS / 32;
-    __shared__ __align__(16) Survivor s_ring[NW][kRing];
-    constexpr bool PACK = (MODE == BLZ_MODE_FIRST) && SINGLE;
-    __shared__ uint4 s_cand[PACK ? NW : 1][PACK ? 2 * 32 * OPT : 1];
-    // the surface table in shared memory, in what static shared memory is left (48 KB per block)
-    constexpr size_t kUsed = sizeof(Survivor) * kRing * NW + (PACK ? sizeof(uint4) * NW * 2 * 32 * OPT : 0);
-    constexpr size_t kLeft = kUsed + 1024 < 48 * 1024 ? 48 * 1024 - 1024 - kUsed : 0;
-    constexpr uint32_t kSurf = kLeft >= 512 * 24 ? 512u : (kLeft >= 256 * 24 ? 256u : (kLeft >= 64 * 24 ? 64u : 1u));
-    __shared__ float4 s_sphere[kSurf];
-    __shared__ uint2 s_lod[kSurf];
+struct DecideSmem {
+    static constexpr int NW = THREADS / 32;
+    static constexpr bool PACK = (MODE == BLZ_MODE_FIRST) && SINGLE;
+    static constexpr size_t kUsed = sizeof(Survivor) * kRing * NW + (PACK ? sizeof(uint4) * NW * 2 * 32 * OPT : 0);
+    static constexpr size_t kLeft = kUsed + 1024 < 48 * 1024 ? 48 * 1024 - 1024 - kUsed : 0;
+    static constexpr uint32_t kSurf = kLeft >= 512 * 24 ? 512u : (kLeft >= 256 * 24 ? 256u : (kLeft >= 64 * 24 ? 64u : 1u));
+    Survivor ring[NW][kRing];
+    uint4 cand[PACK ? NW : 1][PACK ? 2 * 32 * OPT : 1];
+    float4 sphere[kSurf];
+    uint2 lod[kSurf];
+};
+
+// The decide kernels' body: each warp decides chunks of a view (decide_run_warp) and records each
+// chunk's count. kModeFramePyr passes the context's pyramid-ready flag and its wait limit.
+template <int MODE, bool SINGLE, int THREADS, int OPT>
+__device__ __forceinline__ void decide_body(const PipeParams& p, DecideSmem<MODE, SINGLE, THREADS, OPT>& sm,
+                                            const unsigned int* ready = nullptr, uint32_t spinLimit = 0u) {
+    using Smem = DecideSmem<MODE, SINGLE, THREADS, OPT>;
+    constexpr int NW = Smem::NW;
+    constexpr bool PACK = Smem::PACK;
+    constexpr uint32_t kSurf = Smem::kSurf;
     SurfaceCache surf{nullptr, nullptr};
     if (kSurf > 1u && p.sc.surfaceCount <= kSurf) {
         for (uint32_t i = threadIdx.x; i < p.sc.surfaceCount; i += THREADS) {
             const float4* sp = reinterpret_cast<const float4*>(p.sc.surfaces + i);
-            s_sphere[i] = __ldg(sp);
+            sm.sphere[i] = __ldg(sp);
             const uint4 s1 = __ldg(reinterpret_cast<const uint4*>(sp + 1));
-            s_lod[i] = make_uint2(s1.y, s1.z);
+            sm.lod[i] = make_uint2(s1.y, s1.z);
         }
         __syncthreads();
-        surf = SurfaceCache{s_sphere, s_lod};
+        surf = SurfaceCache{sm.sphere, sm.lod};
     }
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t warpsTotal = gridDim.x * NW;
@@ -398,13 +439,13 @@ __global__ void __launch_bounds__(THREADS, (SINGLE || MODE >= 0) ? 1024 / THREAD
         const uint32_t base = (chunk - first) * chunkSize;
         const uint32_t limit = min(base + chunkSize, bv.count);
         uint2* stage = p.staged + static_cast<size_t>(chunk) * chunkSize;
-        Survivor* ring = s_ring[warp];
-        uint4* cand = s_cand[PACK ? warp : 0];
+        Survivor* ring = sm.ring[warp];
+        uint4* cand = sm.cand[PACK ? warp : 0];
         uint32_t total = 0, kept = 0, total1 = 0;
         uint4* keep = nullptr;
         if constexpr (MODE == kModeFrame1) keep = static_cast<uint4*>(p.keep) + 2u * static_cast<size_t>(chunk) * chunkSize;
         uint2* stage1 = nullptr;
-        if constexpr (MODE == kModeFrameFused) stage1 = p.staged2 + static_cast<size_t>(chunk) * chunkSize;
+        if constexpr (fused_mode(MODE)) stage1 = p.staged2 + static_cast<size_t>(chunk) * chunkSize;
         if (MODE == kModeRuntime) {
             switch (bv.mode) {
                 case BLZ_MODE_FIRST: total = decide_run_warp<BLZ_MODE_FIRST, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags, keep, kept); break;
@@ -414,16 +455,54 @@ __global__ void __launch_bounds__(THREADS, (SINGLE || MODE >= 0) ? 1024 / THREAD
             }
         } else {
             total = decide_run_warp<(MODE < 0 ? 0 : MODE), SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags, keep, kept,
-                                                                       stage1, &total1);
+                                                                       stage1, &total1, ready, spinLimit);
         }
         if (lane == 0) {
             p.chunkCount[chunk] = total;
             if constexpr (MODE == kModeFrame1) p.keepCount[chunk] = kept;
-            if constexpr (MODE == kModeFrameFused) p.chunkCount2[chunk] = total1;
+            if constexpr (fused_mode(MODE)) p.chunkCount2[chunk] = total1;
         }
         chunk = next;
     }
     if (flags) atomicOr(&p.scratch->status, flags);
+}
+
+template <int MODE, bool SINGLE, int THREADS, int OPT>
+__global__ void __launch_bounds__(THREADS, (SINGLE || MODE >= 0) ? 1024 / THREADS : 1) cull_decide_kernel(const PipeParams p) {
+    __shared__ DecideSmem<MODE, SINGLE, THREADS, OPT> sm;
+    decide_body<MODE, SINGLE, THREADS, OPT>(p, sm);
+}
+
+// The one-call frame with its pyramid (blz_cull_frame given a depth buffer) in one launch. Each
+// block first takes pyramid tiles by ticket until none is left, building each with the pyramid
+// kernel's block steps in the shared memory its survivor rings use later; the block that finishes
+// the last tile builds the top levels and publishes the pyramid (the context's ready flag). Then the
+// block's warps run the fused sweep, each waiting for the flag before its first Hi-Z test. Tiles go
+// to running blocks only, and a block waits for nothing while it builds, so every tile a warp waits
+// for belongs to a block that is running; the waits are bounded all the same. The frame's scatter
+// rewinds the ticket, the tile count and the flag.
+template <uint32_t HIZ, int THREADS, int OPT>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) cull_frame_kernel(const PipeParams p,
+                                                                           const __grid_constant__ PyramidBuildParams bp) {
+    using Smem = DecideSmem<kModeFramePyr, true, THREADS, OPT>;
+    __shared__ Smem sm;
+    static_assert(sizeof(sm.ring) >= sizeof(float) * (kPyrSmemA + kPyrSmemB), "the tile buffers live in the rings");
+    float* sA = reinterpret_cast<float*>(&sm.ring[0][0]);
+    float* sB = sA + kPyrSmemA;
+    __shared__ uint32_t s_tile;
+    Scratch* scr = p.scratch;
+    const uint32_t tilesX = (bp.width + kPyrTile - 1) / kPyrTile;
+    const uint32_t tiles = tilesX * ((bp.height + kPyrTile - 1) / kPyrTile);
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(&scr->frameTicket, 1u);
+        __syncthreads();
+        const uint32_t t = s_tile;
+        if (t >= tiles) break;
+        pyramid_tile<HIZ, THREADS>(bp, (t % tilesX) * kPyrTile, (t / tilesX) * kPyrTile, sA, sB);
+        pyramid_tile_finish<HIZ, THREADS>(bp, tiles, &scr->frameTilesDone, &scr->frameReady, sA, sB);
+        __syncthreads();  // s_tile and the tile buffers are free again
+    }
+    decide_body<kModeFramePyr, true, THREADS, OPT>(p, sm, &scr->frameReady, bp.spinLimit);
 }
 
 // ------------------------------------------------------------------ scatter kernel
@@ -554,9 +633,16 @@ __global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const 
     scatter_block<SINGLE>(p, blockIdx.x);
 }
 
-// Both record lists of a kept frame in one launch: blocks [0, blocks1) scatter list 1, the rest list 2.
+// Both record lists of a one-call frame in one launch: blocks [0, blocks1) scatter list 1, the rest
+// list 2. Block 0 also rewinds the frame kernel's pyramid ticket, tile count and ready flag (the
+// frame kernel has finished: this launch follows it on the stream).
 __global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter2_kernel(const PipeParams p1, const PipeParams p2,
                                                                            const uint32_t blocks1) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        p1.scratch->frameTicket = 0u;
+        p1.scratch->frameTilesDone = 0u;
+        p1.scratch->frameReady = 0u;
+    }
     if (blockIdx.x < blocks1) scatter_block<true>(p1, blockIdx.x);
     else scatter_block<true>(p2, blockIdx.x - blocks1);
 }
@@ -707,6 +793,47 @@ cudaError_t launch_frame_fused(const PipeParams& p, uint32_t threads, uint32_t o
     if (threads == 128 && opt == 4) return launch_decide_t<kModeFrameFused, true, 128, 4>(q, 0, smCount, s);
     if (threads == 512 && opt == 1) return launch_decide_t<kModeFrameFused, true, 512, 1>(q, 0, smCount, s);
     return launch_decide_t<kModeFrameFused, true, kObjThreads, kObjOpt>(q, 0, smCount, s);
+}
+
+template <uint32_t HIZ, int THREADS, int OPT>
+static cudaError_t launch_frame_pyr_t(const PipeParams& p, const PyramidBuildParams& bp, int smCount, cudaStream_t s) {
+    auto kern = cull_frame_kernel<HIZ, THREADS, OPT>;
+    static const uint32_t occ = [&] {
+        int o = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, THREADS, 0) != cudaSuccess) {
+            (void)cudaGetLastError();
+            o = 1;
+        }
+        return static_cast<uint32_t>(o < 1 ? 1 : o);
+    }();
+    // one warp per chunk at most, but enough blocks (up to one wave) to build the pyramid's tiles
+    const uint32_t wave = occ * static_cast<uint32_t>(smCount > 0 ? smCount : 1);
+    const uint32_t tiles = ((bp.width + kPyrTile - 1) / kPyrTile) * ((bp.height + kPyrTile - 1) / kPyrTile);
+    uint32_t grid = (p.totalTiles + THREADS / 32 - 1) / (THREADS / 32);
+    if (grid < tiles) grid = tiles;
+    if (grid > wave) grid = wave;
+    if (grid == 0) grid = 1;
+    kern<<<grid, THREADS, 0, s>>>(p, bp);
+    return cudaGetLastError();
+}
+
+template <uint32_t HIZ>
+static cudaError_t launch_frame_pyr_hiz(const PipeParams& q, const PyramidBuildParams& bp, uint32_t threads, uint32_t opt,
+                                        int smCount, cudaStream_t s) {
+    if (threads == 256 && opt == 1) return launch_frame_pyr_t<HIZ, 256, 1>(q, bp, smCount, s);
+    if (threads == 256 && opt == 4) return launch_frame_pyr_t<HIZ, 256, 4>(q, bp, smCount, s);
+    if (threads == 128 && opt == 2) return launch_frame_pyr_t<HIZ, 128, 2>(q, bp, smCount, s);
+    if (threads == 128 && opt == 4) return launch_frame_pyr_t<HIZ, 128, 4>(q, bp, smCount, s);
+    if (threads == 512 && opt == 1) return launch_frame_pyr_t<HIZ, 512, 1>(q, bp, smCount, s);
+    return launch_frame_pyr_t<HIZ, kObjThreads, kObjOpt>(q, bp, smCount, s);
+}
+
+cudaError_t launch_frame_pyr(const PipeParams& p, const PyramidBuildParams& bp, uint32_t threads, uint32_t opt, int smCount,
+                             cudaStream_t s) {
+    PipeParams q = p;
+    q.descending = 0u;
+    if (bp.mode == BLZ_HIZ_VULKAN) return launch_frame_pyr_hiz<BLZ_HIZ_VULKAN>(q, bp, threads, opt, smCount, s);
+    return launch_frame_pyr_hiz<BLZ_HIZ_D3D12>(q, bp, threads, opt, smCount, s);
 }
 
 constexpr int kFrameLateThreads = 256;

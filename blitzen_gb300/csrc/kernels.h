@@ -62,6 +62,10 @@ constexpr int kModeFrame1 = 4;
 // frame, inside the frustum and not occluded) or in neither; its visibility is rewritten as pass 2
 // rewrites it. Pass 1's records are staged in staged2 / chunkCount2.
 constexpr int kModeFrameFused = 5;
+// kModeFrameFused with the pyramid built inside the same launch (blz_cull_frame given a depth
+// buffer): the kernel's blocks first build the pyramid's tiles, taken by ticket, and a warp waits
+// for the finished pyramid (a flag in the context's scratch) before its first Hi-Z test.
+constexpr int kModeFramePyr = 6;
 
 constexpr int kObjThreads = 256;
 constexpr int kObjOpt = 2;
@@ -186,7 +190,7 @@ struct PyramidBuildParams {
     uint32_t mipOffset[BLZ_PYRAMID_MAX_MIPS];
     unsigned int* done;  // the context's finished-tile counter (zero between builds)
     uint32_t vec4;       // D3D12: depth rows read 16 bytes at a time (width % 4 == 0, height >= 2, aligned buffers)
-    uint32_t pad;
+    uint32_t spinLimit;  // one-call frame kernel: polls of the pyramid-ready flag before a warp gives up
 };
 
 // Launches a kernel with programmatic stream serialization: it may be scheduled while the kernel
@@ -226,6 +230,8 @@ cudaError_t launch_frame_scatter2(const PipeParams& p1, const PipeParams& p2, cu
 // The fused sweep of blz_cull_frame (kModeFrameFused) after the pyramid: p stages pass 2's records in
 // staged / chunkCount and pass 1's in staged2 / chunkCount2; no scatter.
 cudaError_t launch_frame_fused(const PipeParams& p, uint32_t threads, uint32_t opt, int smCount, cudaStream_t s);
+cudaError_t launch_frame_pyr(const PipeParams& p, const PyramidBuildParams& bp, uint32_t threads, uint32_t opt, int smCount,
+                             cudaStream_t s);
 bool batch_shape_supported(uint32_t threads, uint32_t opt);
 // mode: the pass every view of the batch runs, or -1 when they differ (the kernel reads it per view)
 cudaError_t launch_batch_cull(const PipeParams& p, uint32_t threads, uint32_t opt, uint32_t blocksPerSm, int smCount,

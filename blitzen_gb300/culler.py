@@ -341,6 +341,11 @@ class Culler:
         """Test hook: the next ticket-taking launch starts past n places, so its waits run out."""
         check(self.lib.blz_ctx_debug_advance_ticket(self.ctx, n, _stream_ptr(stream)), "blz_ctx_debug_advance_ticket")
 
+    def debug_skip_frame_tiles(self, n: int, stream=None) -> None:
+        """Test hook: the next cull_frame with a depth buffer skips the pyramid's first n tiles, so its
+        warps time out waiting for the pyramid (blz_ctx_debug_skip_frame_tiles)."""
+        check(self.lib.blz_ctx_debug_skip_frame_tiles(self.ctx, n, _stream_ptr(stream)), "blz_ctx_debug_skip_frame_tiles")
+
     @property
     def launches(self) -> int:
         return int(self.lib.blz_ctx_launch_count(self.ctx))

@@ -91,13 +91,15 @@ const char* blz_version(void);
  * the validation it never had (vulkanData.h:196-197). */
 int blz_ctx_check(blz_ctx* ctx, blz_stream_t stream, uint32_t* flagsOut);
 
-/* Bound of the device-side waits of this context's launches. The one kernel that waits is the
- * single-kernel instanced cull (scenes of more than 1,024 LODs): a tile waits, per LOD, for the
- * running totals of the tiles that started before it, polling one state at most `polls` times;
- * then it gives up, raises BLZ_FLAG_TIMEOUT and finishes without waiting (its results are then
- * wrong; blz_ctx_check returns BLZ_ERR_TIMEOUT and resets the protocol). 0 restores the default
- * (2^20 polls, about a second at worst). Stands in for the bounded fence wait of the reference's
- * frame loop (vulkanData.h:196-197, ce_fenceTimeout). */
+/* Bound of the device-side waits of this context's launches. Two kernels wait:
+ *  - the single-kernel instanced cull (scenes of more than 1,024 LODs): a tile waits, per LOD, for
+ *    the running totals of the tiles that started before it;
+ *  - the one-call frame given a depth buffer (blz_cull_frame): a warp waits, before its first Hi-Z
+ *    test, for the pyramid the launch's blocks build first.
+ * Each polls one word at most `polls` times; then it gives up, raises BLZ_FLAG_TIMEOUT and finishes
+ * without waiting (its results are then wrong; blz_ctx_check returns BLZ_ERR_TIMEOUT and resets the
+ * instanced protocol). 0 restores the default (2^20 polls, about a second at worst). Stands in for
+ * the bounded fence wait of the reference's frame loop (vulkanData.h:196-197, ce_fenceTimeout). */
 int blz_ctx_set_wait_limit(blz_ctx* ctx, uint32_t polls);
 
 /* Test hook for the timeout path only: advances the context's block-ticket counter by n (1..1024)
@@ -106,6 +108,13 @@ int blz_ctx_set_wait_limit(blz_ctx* ctx, uint32_t polls);
  * BLZ_FLAG_TIMEOUT; the launch's last block rewinds the counter, so the launch after it is whole
  * again. No counterpart in the reference. */
 int blz_ctx_debug_advance_ticket(blz_ctx* ctx, uint32_t n, blz_stream_t stream);
+
+/* Test hook for the one-call frame's wait only: advances the context's pyramid-tile ticket by n
+ * (1..1024) on the stream, so that the next blz_cull_frame given a depth buffer never builds the
+ * pyramid's first n tiles. Its warps then wait for a pyramid that is never finished, give up after
+ * the wait limit and raise BLZ_FLAG_TIMEOUT (their records are then wrong); the frame's last launch
+ * rewinds the ticket, so the frame after it is whole again. No counterpart in the reference. */
+int blz_ctx_debug_skip_frame_tiles(blz_ctx* ctx, uint32_t n, blz_stream_t stream);
 
 /* Number of this library's kernel launches enqueued by the context so far. */
 uint64_t blz_ctx_launch_count(const blz_ctx* ctx);
@@ -283,8 +292,10 @@ int blz_frame_late(blz_ctx* ctx, const BlzPyramid* pyramid, const BlzCullTarget*
  * frame, inside the frustum, not occluded) or neither, rewriting the visibility as pass 2 does; one
  * final launch writes both record lists. Same records, counts, pyramid and visibility as
  * blz_cull_first + blz_pyramid_build + blz_cull_late on the same inputs. It keeps nothing for
- * blz_frame_late. dDepth NULL: the pyramid is used as it stands (a caller that built it itself,
- * with blz_pyramid_build earlier or from another frame's depth). Replaces the pass order of
+ * blz_frame_late. With dDepth, the launch's blocks build the pyramid's tiles before their share of
+ * the sweep and each warp waits for the finished pyramid before its first Hi-Z test (a bounded
+ * wait, see blz_ctx_set_wait_limit). dDepth NULL: the pyramid is used as it stands (a caller that
+ * built it itself, with blz_pyramid_build earlier or from another frame's depth). Replaces the pass order of
  * VulkanRenderer::DrawFrame (vulkanDraw.cpp:1015-1031) and dx12Draw.cpp:590-641 minus the draws. */
 int blz_cull_frame(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list, uint32_t* dVisibility,
                    const float* dDepth, const BlzPyramid* pyramid, const BlzCullTarget* pass1Target,
