@@ -10,14 +10,17 @@ Inputs are resident in HBM when the timed region starts; before each step the vi
 restored to the 50% mask and L2 is flushed (a 512 MiB read), both outside the timed events.
 
 value  = objects per second of the device-timed frames: each step replays blz_cull_frame (recorded
-         once with blz_capture_begin/end) as one CUDA graph between two CUDA events. The frame's
+         once with blz_capture_begin/end) as one CUDA graph between two CUDA events. That frame is
+         two launches: one building the pyramid's tiles and then deciding both passes for every
+         object in one sweep, one writing both record lists. The frame's
          other forms (blz_frame_first + blz_pyramid_build + blz_frame_late; blz_cull_first +
          blz_pyramid_build + blz_cull_late) are timed the same way in `frame_forms`, and every part
          as its own graph in `roofline.others`. All three forms give the same records, counts,
          pyramid and visibility, checked against the oracle (`bit_exact`).
 roofline = the headline frame's sweep (blz_cull_frame over the pyramid already built: the decide
          launch for both passes and the launch writing both record lists), algorithmic bytes over
-         its CUDA-event time, against the measured copy bandwidth.
+         its CUDA-event time, against the measured copy bandwidth. `others.frame` is the whole
+         frame against its bytes, pyramid included.
 e2e    = the same frame through the C ABI with host buffers, all inside the timed region: the host
          writes the 1,000 dynamic transform rows into a pinned buffer and replays the recorded step
          (blz_graph_launch): the 8.3 MB depth upload and the pyramid run beside blz_frame_first,
@@ -290,8 +293,9 @@ def main():
     side = torch.cuda.Stream(dev)  # graphs are captured from, and replayed on, a non-default stream
 
     # The frame in the library's three forms, each one step of the workload:
-    #   one_call        blz_cull_frame: pass 1 over every object (keeping the frustum survivors),
-    #                   the pyramid, the survivors' pyramid test, both record lists in one launch
+    #   one_call        blz_cull_frame: the pyramid's tiles, then one sweep deciding both passes for
+    #                   every object (each warp waits for the finished pyramid before its first Hi-Z
+    #                   test), then both record lists in one launch
     #   kept_frame      blz_frame_first, blz_pyramid_build, blz_frame_late (the renderer's order)
     #   separate_calls  blz_cull_first, blz_pyramid_build, blz_cull_late (each pass on its own)
     def frame_one_call():
@@ -416,12 +420,13 @@ def main():
                 "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
                 "traffic": None, "algorithmic_bytes": bytes_sweep, "ms": t_sw,
                 "ms_note": "blz_cull_frame with no depth (the pyramid already built) recorded as its own graph: "
-                           "the headline frame minus its pyramid launch",
+                           "the headline frame without its pyramid tiles",
                 "others": {
                     "frame": {"ms": t_step, "bytes": bytes_frame, "GB/s": gbs(bytes_frame, t_step),
                               "frac": gbs(bytes_frame, t_step) / peak,
-                              "note": "blz_cull_frame; bytes: every object's tables and visibility read once, "
-                                      "visibility written once, both record lists, the pyramid"},
+                              "note": "blz_cull_frame (the timed step; the pyramid built inside its sweep launch); "
+                                      "bytes: every object's tables and visibility read once, visibility written "
+                                      "once, both record lists, the depth buffer read and the pyramid written"},
                     "frame_first": {"ms": t_part["frame_first"], "bytes": bytes_a,
                                     "GB/s": gbs(bytes_a, t_part["frame_first"]),
                                     "frac": gbs(bytes_a, t_part["frame_first"]) / peak,
