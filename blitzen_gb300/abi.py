@@ -116,7 +116,7 @@ class BatchView(C.Structure):
 
 class LaunchShape(C.Structure):
     _fields_ = [("threadsPerBlock", C.c_uint32), ("objectsPerThread", C.c_uint32),
-                ("blocksPerSm", C.c_uint32), ("reserved", C.c_uint32)]
+                ("blocksPerSm", C.c_uint32), ("chunkObjects", C.c_uint32)]
 
 
 class ServeConfig(C.Structure):
@@ -198,6 +198,8 @@ _PROTOS = {
     "blz_get_launch_shape": (_I, [_P, C.POINTER(LaunchShape)]),
     "blz_set_launch_shape": (_I, [_P, C.POINTER(LaunchShape)]),
     "blz_autotune_batch": (_I, [_P, C.POINTER(BatchView), _U32, _U32, _P, C.POINTER(LaunchShape), C.POINTER(C.c_float)]),
+    "blz_autotune_single": (_I, [_P, C.POINTER(CameraViewData), RenderList, _U32, _P, C.POINTER(Pyramid),
+                                 C.POINTER(CullTarget), _U32, _P, C.POINTER(LaunchShape), C.POINTER(C.c_float)]),
     "blz_capture_begin": (_I, [_P, _P]),
     "blz_capture_end": (_I, [_P, _P, C.POINTER(_P), C.POINTER(_U32)]),
     "blz_graph_launch": (_I, [_P, _P]),

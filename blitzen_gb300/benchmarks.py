@@ -83,8 +83,8 @@ def _time(fn, reps, stream):
 
 def batched_views(culler, scene, device, n_views=64, reps=20, shape=None) -> dict:
     """64 views of log-uniform size over the resident scene: one batched launch (and its graph)
-    against one launch per view. shape = (threads, objects per thread, blocks per SM) fixes the
-    launch shape; by default the autotuner picks it."""
+    against one launch per view. shape = (threads, objects per thread, blocks per SM[, objects per
+    chunk]) fixes the launch shape; by default the autotuner picks it and its chunk size."""
     lib = abi.load()
     views, keep, total = build_views(culler, scene, device, n_views)
     stream = torch.cuda.current_stream(device)
@@ -102,7 +102,7 @@ def batched_views(culler, scene, device, n_views=64, reps=20, shape=None) -> dic
     if shape is None:  # autotuned launch shape for this batch
         abi.check(lib.blz_autotune_batch(culler.ctx, views, n_views, 3, sp, C.byref(best), C.byref(us)), "autotune")
     else:
-        best = abi.LaunchShape(shape[0], shape[1], shape[2], 0)
+        best = abi.LaunchShape(shape[0], shape[1], shape[2], shape[3] if len(shape) > 3 else 0)
         abi.check(lib.blz_set_launch_shape(culler.ctx, C.byref(best)), "launch shape")
 
     # parity: batched == per-view, record by record, before timing the batch
@@ -124,7 +124,8 @@ def batched_views(culler, scene, device, n_views=64, reps=20, shape=None) -> dic
     return {
         "views": n_views, "objects": total, "identical_to_per_view": identical,
         "launch_shape": {"threads": best.threadsPerBlock, "objects_per_thread": best.objectsPerThread,
-                         "blocks_per_sm": best.blocksPerSm},
+                         "blocks_per_sm": best.blocksPerSm, "chunk_objects": best.chunkObjects or 512,
+                         "autotune_us": float(us.value) if shape is None else None},
         "batched_graph_ms": t_graph, "batched_ms": t_batch, "per_view_ms": t_per,
         "batched_objects_per_s": total / (t_graph * 1e-3), "per_view_objects_per_s": total / (t_per * 1e-3),
         "speedup": t_per / t_graph,

@@ -550,7 +550,13 @@ static int object_cull(blz_ctx* c, uint32_t mode, const BlzCameraViewData* view,
         rc = check_pyramid(pyr, true);
         if (rc != BLZ_OK) return rc;
     }
-    const uint32_t tile = single_chunk_size(mode, c->singleThreads, c->singleOpt, count, c->smCount);
+    // the single-view autotuner's choice for this size and pass, else the context's shape
+    uint32_t threads = c->singleThreads, opt = c->singleOpt;
+    if (const TunedShape* t = find_tuned(c, count, 1u, mode)) {
+        threads = t->shape.threadsPerBlock;
+        opt = t->shape.objectsPerThread;
+    }
+    const uint32_t tile = single_chunk_size(mode, threads, opt, count, c->smCount);
     uint32_t tiles = (count + tile - 1) / tile;
     if (tiles == 0) tiles = 1;  // an empty list still gets one chunk, and its draw count is written
     rc = ensure_chunk_scratch(c, tiles, tile);
@@ -576,10 +582,82 @@ static int object_cull(blz_ctx* c, uint32_t mode, const BlzCameraViewData* view,
     p.chunkSize = tile;
     bind_chunk_scratch(c, p);
     p.workCounter = nullptr;  // one chunk per resident warp, assigned by warp index
-    cudaError_t e = launch_object_cull(mode, p, c->singleThreads, c->singleOpt, c->smCount, reinterpret_cast<cudaStream_t>(stream));
+    cudaError_t e = launch_object_cull(mode, p, threads, opt, c->smCount, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "cull launch");
     c->launches += 2;  // decide + scatter
     return BLZ_OK;
+}
+
+// The single-view autotuner: every single-view shape timed on the caller's pass, each run on a copy
+// of the visibility buffer (restored before every run, outside the timed events).
+static int autotune_single(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, uint32_t mode, const uint32_t* vis,
+                           const BlzPyramid* pyr, const BlzCullTarget* target, uint32_t repeats, blz_stream_t stream,
+                           BlzLaunchShape* best, float* bestUs) {
+    if (!c || !view) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or view is NULL");
+    if (mode > BLZ_MODE_TEMPORAL) return fail(BLZ_ERR_INVALID_ARGUMENT, "unknown mode %u", mode);
+    if (c->capturing) return fail(BLZ_ERR_INVALID_ARGUMENT, "the autotuner cannot run inside a capture");
+    const BlzRenderObject* objs = nullptr;
+    uint32_t count = 0;
+    int rc = resolve_list(c, list, &objs, &count);
+    if (rc != BLZ_OK) return rc;
+    if (count == 0) return fail(BLZ_ERR_INVALID_ARGUMENT, "nothing to tune on: the list is empty");
+    if ((mode == BLZ_MODE_FIRST || mode == BLZ_MODE_LATE) && !vis) return fail(BLZ_ERR_INVALID_ARGUMENT, "visibility buffer is NULL");
+    auto report = [&](const TunedShape& t) {
+        if (best) {
+            *best = t.shape;
+            best->chunkObjects = single_chunk_size(mode, t.shape.threadsPerBlock, t.shape.objectsPerThread, count, c->smCount);
+        }
+        if (bestUs) *bestUs = t.us;
+        return BLZ_OK;
+    };
+    if (const TunedShape* t = find_tuned(c, count, 1u, mode)) return report(*t);
+    if (repeats == 0) repeats = 5;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    uint32_t* work = nullptr;  // the pass's visibility buffer: a copy of the caller's
+    if (vis && cudaMalloc(&work, sizeof(uint32_t) * count) != cudaSuccess) return fail(BLZ_ERR_OUT_OF_MEMORY, "autotune visibility copy");
+    BlzRenderList own{objs, count};
+    const uint32_t shapes[][2] = {{256, 1}, {256, 2}, {256, 4}, {128, 2}, {128, 4}, {512, 1}};
+    const uint32_t savedT = c->singleThreads, savedO = c->singleOpt;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    TunedShape top{count, 1u, mode, BlzLaunchShape{savedT, savedO, 0, 0}, 1e30f};
+    for (const auto& sh : shapes) {
+        c->singleThreads = sh[0];
+        c->singleOpt = sh[1];
+        float total = 0.f;
+        rc = BLZ_OK;
+        for (uint32_t r = 0; r <= repeats && rc == BLZ_OK; ++r) {  // run 0 is untimed
+            if (work && cudaMemcpyAsync(work, vis, sizeof(uint32_t) * count, cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+                rc = fail(BLZ_ERR_CUDA, "autotune visibility copy");
+                break;
+            }
+            cudaEventRecord(a, st);
+            rc = object_cull(c, mode, view, own, work, pyr, target, stream);
+            cudaEventRecord(b, st);
+            cudaEventSynchronize(b);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (r > 0) total += ms;
+        }
+        if (rc != BLZ_OK) break;
+        const float us = total * 1000.f / static_cast<float>(repeats);
+        if (us < top.us) {
+            top.us = us;
+            top.shape = BlzLaunchShape{sh[0], sh[1], 0, 0};
+        }
+    }
+    c->singleThreads = savedT;
+    c->singleOpt = savedO;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (work) {
+        cudaStreamSynchronize(st);
+        cudaFree(work);
+    }
+    if (rc != BLZ_OK) return rc;
+    remember_tuned(c, top);
+    return report(top);
 }
 
 int blz_cull_frustum(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, const BlzCullTarget* target, blz_stream_t s) {
@@ -599,6 +677,12 @@ int blz_cull_late(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list,
 int blz_cull_temporal(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, const BlzPyramid* pyr,
                       const BlzCullTarget* target, blz_stream_t s) {
     return object_cull(c, BLZ_MODE_TEMPORAL, view, list, nullptr, pyr, target, s);
+}
+
+int blz_autotune_single(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList list, uint32_t mode, const uint32_t* vis,
+                        const BlzPyramid* pyr, const BlzCullTarget* target, uint32_t repeats, blz_stream_t stream,
+                        BlzLaunchShape* best, float* bestUs) {
+    return autotune_single(c, view, list, mode, vis, pyr, target, repeats, stream, best, bestUs);
 }
 
 // ------------------------------------------------------------------ kept frames

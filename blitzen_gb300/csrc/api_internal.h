@@ -16,6 +16,17 @@ constexpr size_t kDefaultStateCapacity = size_t(1) << 22;  // 4M tile states (32
 constexpr size_t kPinnedBytes = size_t(8) << 20;            // pinned host staging: transform rows, batch views
 constexpr uint32_t kMaxInstancedLods = 4096;                // shared-memory bucket histograms
 
+// An autotuner's choice for one workload size: batches keyed by (total objects, views), single-view
+// passes by (objects, 1, pass).
+constexpr uint32_t kTunedBatch = 0xFFFFFFFFu;
+struct TunedShape {
+    uint64_t objects;
+    uint32_t views;
+    uint32_t mode;  // the single-view pass, or kTunedBatch
+    BlzLaunchShape shape;
+    float us;
+};
+
 }  // namespace blz
 
 struct blz_ctx {
@@ -46,6 +57,7 @@ struct blz_ctx {
     bool capturing = false;            // a blz_capture_begin is open
     uint64_t launchesAtCapture = 0;
     BlzLaunchShape shape{256, 2, 0, 0};   // batch launches
+    std::vector<blz::TunedShape> tuned;  // the autotuners' cached choices (cleared by blz_set_launch_shape)
     uint32_t singleThreads = 256, singleOpt = 2;  // single-view launches
     uint32_t waitLimit = static_cast<uint32_t>(blz::kSpinLimitDefault);  // polls before a device-side wait gives up
     unsigned char* noallocBase = nullptr;  // device address of the no-alloc staging array, fetched by this context's first no-alloc call
@@ -74,5 +86,9 @@ int ensure_states(blz_ctx* c, size_t states);
 // grows it synchronises the device first).
 int ensure_chunk_scratch(blz_ctx* c, size_t chunks, size_t chunkSize);
 void bind_chunk_scratch(blz_ctx* c, PipeParams& p);
+
+// The cached autotuner choice for (objects, views, mode), or null.
+const TunedShape* find_tuned(const blz_ctx* c, uint64_t objects, uint32_t views, uint32_t mode);
+void remember_tuned(blz_ctx* c, const TunedShape& t);
 
 }  // namespace blz

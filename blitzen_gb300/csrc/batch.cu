@@ -2,8 +2,8 @@
 // and the launch-shape autotuner.
 //
 // The reference culls one camera per pass with one dispatch each (src/Core/blitzenEngine.h:49,
-// src/Renderer/BlitzenVulkan/vulkanDraw.cpp:107-226). Here every (view, 512-object chunk) pair is
-// an item of one decide launch: warps start on the chunk of their index and take further chunks
+// src/Renderer/BlitzenVulkan/vulkanDraw.cpp:107-226). Here every (view, chunk) pair is an item of
+// one decide launch (chunks of 256, 512 or 1024 objects, the launch shape's chunk size): warps start on the chunk of their index and take further chunks
 // from a work counter, and the scatter launch turns the per-chunk counts into per-view offsets and
 // draw counts, so views of 1k and 2M objects share the machine without a launch or a tail per view.
 #include <algorithm>
@@ -14,6 +14,39 @@
 #include "api_internal.h"
 
 namespace blz {
+
+// Objects per chunk of a batch launch shape (0: the default).
+static uint32_t batch_chunk(const BlzLaunchShape& s) { return s.chunkObjects ? s.chunkObjects : object_tile_size(); }
+
+static bool chunk_supported(uint32_t chunk) { return chunk == 0 || chunk == 256 || chunk == 512 || chunk == 1024; }
+
+const TunedShape* find_tuned(const blz_ctx* c, uint64_t objects, uint32_t views, uint32_t mode) {
+    for (const TunedShape& t : c->tuned)
+        if (t.objects == objects && t.views == views && t.mode == mode) return &t;
+    return nullptr;
+}
+
+void remember_tuned(blz_ctx* c, const TunedShape& t) {
+    for (TunedShape& u : c->tuned)
+        if (u.objects == t.objects && u.views == t.views && u.mode == t.mode) {
+            u = t;
+            return;
+        }
+    c->tuned.push_back(t);
+}
+
+// Total objects of a batch (each view's list, or the scene's when the list is NULL).
+static uint64_t batch_objects(const blz_ctx* c, const BlzBatchView* views, uint32_t n) {
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < n; ++i) total += views[i].list.objects ? views[i].list.count : c->defaultCount;
+    return total;
+}
+
+// The shape a batch of these views runs with: the autotuner's choice for its size, else the context's.
+static BlzLaunchShape batch_shape(const blz_ctx* c, const BlzBatchView* views, uint32_t n) {
+    const TunedShape* t = find_tuned(c, batch_objects(c, views, n), n, kTunedBatch);
+    return t ? t->shape : c->shape;
+}
 
 static int build_views(blz_ctx* c, const BlzBatchView* views, uint32_t n, uint32_t tile, std::vector<BatchViewDev>& out,
                        std::vector<uint32_t>& tileStart) {
@@ -65,7 +98,7 @@ static int build_views(blz_ctx* c, const BlzBatchView* views, uint32_t n, uint32
 static size_t batch_bytes(uint32_t n) { return sizeof(BatchViewDev) * n + sizeof(uint32_t) * (n + 1) + 256; }
 
 static int upload_views(blz_ctx* c, const std::vector<BatchViewDev>& d, const std::vector<uint32_t>& ts, void* dst,
-                        cudaStream_t st, PipeParams& p) {
+                        cudaStream_t st, uint32_t tile, PipeParams& p) {
     const uint32_t n = static_cast<uint32_t>(d.size());
     const size_t viewsBytes = sizeof(BatchViewDev) * n;
     const size_t tsOff = (viewsBytes + 255) & ~size_t(255);
@@ -84,7 +117,7 @@ static int upload_views(blz_ctx* c, const std::vector<BatchViewDev>& d, const st
     p.tileStart = reinterpret_cast<const uint32_t*>(static_cast<char*>(dst) + tsOff);
     p.viewCount = n;
     p.totalTiles = ts[n];
-    p.chunkSize = object_tile_size();
+    p.chunkSize = tile;
     p.scratch = c->scratch;
     return BLZ_OK;
 }
@@ -110,10 +143,8 @@ static int uniform_mode(const BlzBatchView* views, uint32_t n) {
     return n ? static_cast<int>(views[0].mode) : -1;
 }
 
-int run_batch(blz_ctx* c, const BlzBatchView* views, uint32_t n, cudaStream_t st) {
-    if (!c || (n && !views)) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or views is NULL");
-    if (n == 0) return BLZ_OK;
-    const uint32_t tile = object_tile_size();
+static int run_batch_shape(blz_ctx* c, const BlzBatchView* views, uint32_t n, cudaStream_t st, const BlzLaunchShape& sh) {
+    const uint32_t tile = batch_chunk(sh);
     std::vector<BatchViewDev> d;
     std::vector<uint32_t> ts;
     int rc = build_views(c, views, n, tile, d, ts);
@@ -123,14 +154,20 @@ int run_batch(blz_ctx* c, const BlzBatchView* views, uint32_t n, cudaStream_t st
     rc = ensure_chunk_scratch(c, ts[n], tile);
     if (rc != BLZ_OK) return rc;
     PipeParams p{};
-    rc = upload_views(c, d, ts, c->batchDev, st, p);
+    rc = upload_views(c, d, ts, c->batchDev, st, tile, p);
     if (rc != BLZ_OK) return rc;
     bind_chunk_scratch(c, p);
-    cudaError_t e = launch_batch_cull(p, c->shape.threadsPerBlock, c->shape.objectsPerThread, c->shape.blocksPerSm, c->smCount, st,
+    cudaError_t e = launch_batch_cull(p, sh.threadsPerBlock, sh.objectsPerThread, sh.blocksPerSm, c->smCount, st,
                                       uniform_mode(views, n));
     if (e != cudaSuccess) return cuda_fail(e, "batch launch");
     c->launches += 2;  // decide + scatter
     return BLZ_OK;
+}
+
+int run_batch(blz_ctx* c, const BlzBatchView* views, uint32_t n, cudaStream_t st) {
+    if (!c || (n && !views)) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or views is NULL");
+    if (n == 0) return BLZ_OK;
+    return run_batch_shape(c, views, n, st, batch_shape(c, views, n));
 }
 
 }  // namespace blz
@@ -209,11 +246,12 @@ int blz_cull_batch_per_view(blz_ctx* c, const BlzBatchView* views, uint32_t n, b
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     std::vector<BatchViewDev> d;
     std::vector<uint32_t> ts;
-    int rc = build_views(c, views, n, object_tile_size(), d, ts);
+    const uint32_t tile = batch_chunk(batch_shape(c, views, n));
+    int rc = build_views(c, views, n, tile, d, ts);
     if (rc != BLZ_OK) return rc;
     uint32_t maxTiles = 1;
     for (uint32_t i = 0; i < n; ++i) maxTiles = std::max(maxTiles, ts[i + 1] - ts[i]);
-    rc = ensure_chunk_scratch(c, maxTiles, object_tile_size());
+    rc = ensure_chunk_scratch(c, maxTiles, tile);
     if (rc != BLZ_OK) return rc;
     for (uint32_t i = 0; i < n; ++i) {
         PipeParams p{};
@@ -223,7 +261,7 @@ int blz_cull_batch_per_view(blz_ctx* c, const BlzBatchView* views, uint32_t n, b
         p.tileStart = nullptr;
         p.viewCount = 1;
         p.totalTiles = ts[i + 1] - ts[i];
-        p.chunkSize = object_tile_size();
+        p.chunkSize = tile;
         bind_chunk_scratch(c, p);
         cudaError_t e = launch_object_cull(d[i].mode, p, c->singleThreads, c->singleOpt, c->smCount, st);
         if (e != cudaSuccess) return cuda_fail(e, "per-view cull launch");
@@ -242,7 +280,10 @@ int blz_set_launch_shape(blz_ctx* c, const BlzLaunchShape* s) {
     if (!c || !s) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or shape is NULL");
     if (!batch_shape_supported(s->threadsPerBlock, s->objectsPerThread))
         return fail(BLZ_ERR_INVALID_ARGUMENT, "unsupported launch shape %u x %u", s->threadsPerBlock, s->objectsPerThread);
+    if (!chunk_supported(s->chunkObjects))
+        return fail(BLZ_ERR_INVALID_ARGUMENT, "unsupported chunk size %u (256, 512, 1024 or 0)", s->chunkObjects);
     c->shape = *s;
+    c->tuned.clear();  // an explicit shape wins over every cached choice
     if (single_shape_supported(s->threadsPerBlock, s->objectsPerThread)) {
         c->singleThreads = s->threadsPerBlock;
         c->singleOpt = s->objectsPerThread;
@@ -253,49 +294,63 @@ int blz_set_launch_shape(blz_ctx* c, const BlzLaunchShape* s) {
 int blz_autotune_batch(blz_ctx* c, const BlzBatchView* views, uint32_t n, uint32_t repeats, blz_stream_t stream,
                        BlzLaunchShape* best, float* bestUs) {
     if (!c || !views || n == 0) return fail(BLZ_ERR_INVALID_ARGUMENT, "ctx or views is NULL");
+    if (c->capturing) return fail(BLZ_ERR_INVALID_ARGUMENT, "the autotuner cannot run inside a capture");
+    const uint64_t objects = batch_objects(c, views, n);
+    if (const TunedShape* t = find_tuned(c, objects, n, kTunedBatch)) {
+        c->shape = t->shape;
+        if (best) *best = t->shape;
+        if (bestUs) *bestUs = t->us;
+        return BLZ_OK;
+    }
     if (repeats == 0) repeats = 5;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const uint32_t threads[] = {128, 256, 512};
     const uint32_t opts[] = {1, 2, 4, 8};
     const uint32_t perSm[] = {0, 1, 2, 4};
+    const uint32_t chunks[] = {256, 512, 1024};
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    BlzLaunchShape saved = c->shape, top = saved;
+    BlzLaunchShape top = c->shape;
     float topUs = 1e30f;
     for (uint32_t t : threads)
         for (uint32_t o : opts)
-            for (uint32_t s : perSm) {
-                if (s && s * t > 2048) continue;
-                c->shape = BlzLaunchShape{t, o, s, 0};
-                if (run_batch(c, views, n, st) != BLZ_OK) continue;  // warm-up
-                cudaEventRecord(a, st);
-                int rc = BLZ_OK;
-                for (uint32_t r = 0; r < repeats && rc == BLZ_OK; ++r) rc = run_batch(c, views, n, st);
-                cudaEventRecord(b, st);
-                cudaEventSynchronize(b);
-                if (rc != BLZ_OK) continue;
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, a, b);
-                const float us = ms * 1000.f / static_cast<float>(repeats);
-                if (us < topUs) {
-                    topUs = us;
-                    top = c->shape;
+            for (uint32_t s : perSm)
+                for (uint32_t k : chunks) {
+                    if (s && s * t > 2048) continue;
+                    if (!batch_shape_supported(t, o)) continue;
+                    const BlzLaunchShape sh{t, o, s, k};
+                    if (run_batch_shape(c, views, n, st, sh) != BLZ_OK) continue;  // warm-up
+                    cudaEventRecord(a, st);
+                    int rc = BLZ_OK;
+                    for (uint32_t r = 0; r < repeats && rc == BLZ_OK; ++r) rc = run_batch_shape(c, views, n, st, sh);
+                    cudaEventRecord(b, st);
+                    cudaEventSynchronize(b);
+                    if (rc != BLZ_OK) continue;
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, a, b);
+                    const float us = ms * 1000.f / static_cast<float>(repeats);
+                    if (us < topUs) {
+                        topUs = us;
+                        top = sh;
+                    }
                 }
-            }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    c->shape = (topUs < 1e30f) ? top : saved;
-    if (best) *best = c->shape;
+    if (!(topUs < 1e30f)) return fail(BLZ_ERR_CUDA, "no launch shape ran");
+    c->shape = top;
+    remember_tuned(c, TunedShape{objects, n, kTunedBatch, top, topUs});
+    if (best) *best = top;
     if (bestUs) *bestUs = topUs;
-    return topUs < 1e30f ? BLZ_OK : fail(BLZ_ERR_CUDA, "no launch shape ran");
+    return BLZ_OK;
 }
 
 int blz_batch_graph_create(blz_ctx* c, const BlzBatchView* views, uint32_t n, blz_stream_t stream, blz_batch_graph** outGraph) {
     if (!c || !views || n == 0 || !outGraph) return fail(BLZ_ERR_INVALID_ARGUMENT, "bad batch graph arguments");
     *outGraph = nullptr;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const uint32_t tile = object_tile_size();
+    const BlzLaunchShape sh = batch_shape(c, views, n);
+    const uint32_t tile = batch_chunk(sh);
     std::vector<BatchViewDev> d;
     std::vector<uint32_t> ts;
     int rc = build_views(c, views, n, tile, d, ts);
@@ -308,7 +363,7 @@ int blz_batch_graph_create(blz_ctx* c, const BlzBatchView* views, uint32_t n, bl
         return fail(BLZ_ERR_OUT_OF_MEMORY, "batch graph workspace allocation failed");
     }
     PipeParams p{};
-    rc = upload_views(c, d, ts, g->viewsDev, st, p);
+    rc = upload_views(c, d, ts, g->viewsDev, st, tile, p);
     if (rc == BLZ_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = fail(BLZ_ERR_CUDA, "batch graph upload failed");
     if (rc == BLZ_OK) {
         const size_t chunks = ts[n], objects = chunks * tile;
@@ -328,8 +383,8 @@ int blz_batch_graph_create(blz_ctx* c, const BlzBatchView* views, uint32_t n, bl
         cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            cudaError_t le = launch_batch_cull(p, c->shape.threadsPerBlock, c->shape.objectsPerThread, c->shape.blocksPerSm,
-                                               c->smCount, cap, uniform_mode(views, n));
+            cudaError_t le = launch_batch_cull(p, sh.threadsPerBlock, sh.objectsPerThread, sh.blocksPerSm, c->smCount, cap,
+                                               uniform_mode(views, n));
             e = cudaStreamEndCapture(cap, &g->graph);
             if (le != cudaSuccess) e = le;
         }

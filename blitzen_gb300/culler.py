@@ -307,15 +307,33 @@ class Culler:
 
     # ------------------------------------------------------------------ launch shape
 
-    def set_launch_shape(self, threads: int, objects_per_thread: int, blocks_per_sm: int = 0) -> None:
+    def set_launch_shape(self, threads: int, objects_per_thread: int, blocks_per_sm: int = 0,
+                         chunk_objects: int = 0) -> None:
+        """The batch launch shape (and the single-view one where it has that shape); forgets the
+        autotuners' cached choices (blz_set_launch_shape)."""
         check(self.lib.blz_set_launch_shape(self.ctx, C.byref(abi.LaunchShape(threads, objects_per_thread,
-                                                                              blocks_per_sm, 0))),
+                                                                              blocks_per_sm, chunk_objects))),
               "blz_set_launch_shape")
 
     def launch_shape(self) -> dict:
         s = abi.LaunchShape()
         check(self.lib.blz_get_launch_shape(self.ctx, C.byref(s)), "blz_get_launch_shape")
-        return {"threads": s.threadsPerBlock, "objects_per_thread": s.objectsPerThread, "blocks_per_sm": s.blocksPerSm}
+        return {"threads": s.threadsPerBlock, "objects_per_thread": s.objectsPerThread, "blocks_per_sm": s.blocksPerSm,
+                "chunk_objects": s.chunkObjects or 512}
+
+    def autotune_single(self, view, mode: int, target: Target, visibility: torch.Tensor | None = None,
+                        pyramid: DevicePyramid | None = None, objects=None, count=None, repeats: int = 3,
+                        stream=None) -> tuple[dict, float]:
+        """Times every single-view shape on this pass and caches the fastest for the list's size and the
+        pass (blz_autotune_single); returns (shape, microseconds). The visibility is left as it was."""
+        t = target.ctype()
+        best, us = abi.LaunchShape(), C.c_float(0)
+        check(self.lib.blz_autotune_single(self.ctx, C.byref(view), self._list(objects, count), mode,
+                                           visibility.data_ptr() if visibility is not None else None,
+                                           C.byref(pyramid.desc) if pyramid else None, C.byref(t), repeats,
+                                           _stream_ptr(stream), C.byref(best), C.byref(us)), "blz_autotune_single")
+        return ({"threads": best.threadsPerBlock, "objects_per_thread": best.objectsPerThread,
+                 "chunk_objects": best.chunkObjects}, float(us.value))
 
     # ------------------------------------------------------------------ status
 

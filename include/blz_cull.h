@@ -392,21 +392,39 @@ int blz_batch_graph_set_view(blz_batch_graph* g, uint32_t viewIndex, const BlzCa
 int blz_batch_graph_launch(blz_batch_graph* g, blz_stream_t stream);
 int blz_batch_graph_destroy(blz_batch_graph* g);
 
-/* Launch shape used by the batch kernel (threads per block, objects per thread, blocks per SM).
- * blz_set_launch_shape also sets the single-view kernels' threads and objects per thread when they
- * have that shape (256 x 1, 2 or 4; 128 x 2 or 4; 512 x 1). blz_autotune_batch measures the
- * candidate shapes on the given batch and keeps the fastest for the batch kernel only. A batch
- * whose views all run the same pass uses a kernel compiled for that pass for 256 x 1 and 512 x 1. */
+/* Launch shape used by the batch kernel: threads per block, objects per thread, blocks per SM and
+ * objects per chunk (the compaction unit: each chunk's records are staged and counted together;
+ * 256, 512 or 1024, 0 = 512). blz_set_launch_shape also sets the single-view kernels' threads and
+ * objects per thread when they have that shape (256 x 1, 2 or 4; 128 x 2 or 4; 512 x 1), and
+ * forgets every choice the autotuners cached. A batch whose views all run the same pass uses a
+ * kernel compiled for that pass for 256 x 1 and 512 x 1.
+ *
+ * blz_autotune_batch times every batch shape (threads x objects per thread x blocks per SM x chunk
+ * size) on the given batch, keeps the fastest as the context's shape and caches it for the batch's
+ * size (total objects, view count): later batches of that size use it, whatever the context's
+ * shape, and a later call for that size returns the cached choice without timing again. The
+ * reference has one fixed shape, N/64 + 1 groups of 64 threads (blitML.h:64-67). */
 typedef struct BlzLaunchShape {
     uint32_t threadsPerBlock;
     uint32_t objectsPerThread;
     uint32_t blocksPerSm;
-    uint32_t reserved;
+    uint32_t chunkObjects;
 } BlzLaunchShape;
 int blz_get_launch_shape(const blz_ctx* ctx, BlzLaunchShape* out);
 int blz_set_launch_shape(blz_ctx* ctx, const BlzLaunchShape* shape);
 int blz_autotune_batch(blz_ctx* ctx, const BlzBatchView* views, uint32_t viewCount, uint32_t repeats,
                        blz_stream_t stream, BlzLaunchShape* best, float* bestMicroseconds);
+
+/* Times the single-view pass `mode` (BLZ_MODE_FRUSTUM, FIRST, LATE or TEMPORAL) on the given view,
+ * list, pyramid and target under every single-view shape (256 x 1, 2, 4; 128 x 2, 4; 512 x 1), each
+ * `repeats` times (0: 5) after one untimed run, and caches the fastest for (list size, pass): later
+ * single-view culls of that size and pass use it. The visibility buffer is read but never changed:
+ * each run works on a copy. The target's records and count are overwritten. best gets the shape,
+ * with chunkObjects = the chunk the single-view kernels use for it (one chunk per resident warp);
+ * a second call for the same size and pass returns the cached choice. Refused inside a capture. */
+int blz_autotune_single(blz_ctx* ctx, const BlzCameraViewData* view, BlzRenderList list, uint32_t mode,
+                        const uint32_t* dVisibility, const BlzPyramid* pyramid, const BlzCullTarget* target,
+                        uint32_t repeats, blz_stream_t stream, BlzLaunchShape* best, float* bestMicroseconds);
 
 /* ---------------------------------------------------------------- recorded frames */
 

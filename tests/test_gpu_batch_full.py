@@ -1,6 +1,7 @@
 """The batched-views workload at full size (64 views over the 4M-object stress scene, log-uniform
 1k..2M objects per view, each with its own rasterised depth and pyramid, frustum + Hi-Z + LOD),
-batched in one launch under every supported launch shape, compared view by view with the oracle."""
+batched in one launch under every supported launch shape and every chunk size, compared view by view
+with the oracle."""
 import numpy as np
 import pytest
 
@@ -12,8 +13,13 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(256, 2, 0), (512, 2, 0), (512, 1, 0), (256, 1, 0), (256, 4, 0), (128, 1, 0), (128, 2, 0), (128, 4, 0),
-          (128, 8, 0), (256, 2, 1), (256, 2, 2), (128, 2, 4), (512, 2, 1)]
+# (threads, objects per thread, blocks per SM, objects per chunk): every shape at the default chunk
+# (512), and every chunk size the autotuner can pick (256, 512, 1024) under the extreme shapes
+SHAPES = [(256, 2, 0, 0), (512, 2, 0, 0), (512, 1, 0, 0), (256, 1, 0, 0), (256, 4, 0, 0), (128, 1, 0, 0),
+          (128, 2, 0, 0), (128, 4, 0, 0), (128, 8, 0, 0), (256, 2, 1, 0), (256, 2, 2, 0), (128, 2, 4, 0),
+          (512, 2, 1, 0),
+          (256, 2, 0, 256), (128, 8, 0, 256), (512, 1, 0, 256), (512, 2, 1, 256), (128, 1, 4, 256),
+          (256, 2, 0, 1024), (128, 8, 0, 1024), (512, 1, 0, 1024), (512, 2, 1, 1024), (128, 1, 4, 1024)]
 
 
 @pytest.fixture(scope="module")

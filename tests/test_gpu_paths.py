@@ -336,13 +336,66 @@ def test_batch_graph_replay(stress_ctx):
 
 
 def test_autotune_picks_a_supported_shape(stress_ctx):
+    """blz_autotune_batch picks a shape and a chunk size, caches them for the batch's size (a second
+    call returns the same choice untimed), batches of that size use them and still match the oracle,
+    and an explicit shape forgets the cache."""
     c, sc = stress_ctx
     views, keep, ref = _batch(c, sc, n_views=4, seed=21)
     lib = abi.load()
     best, us = abi.LaunchShape(), C.c_float(0)
     abi.check(lib.blz_autotune_batch(c.ctx, views, len(ref), 2, None, C.byref(best), C.byref(us)), "autotune")
     assert best.threadsPerBlock in (128, 256, 512) and best.objectsPerThread in (1, 2, 4, 8)
+    assert best.chunkObjects in (256, 512, 1024)
     assert us.value > 0
+    again, us2 = abi.LaunchShape(), C.c_float(0)
+    abi.check(lib.blz_autotune_batch(c.ctx, views, len(ref), 2, None, C.byref(again), C.byref(us2)), "autotune")
+    assert (again.threadsPerBlock, again.objectsPerThread, again.blocksPerSm, again.chunkObjects) == \
+        (best.threadsPerBlock, best.objectsPerThread, best.blocksPerSm, best.chunkObjects)
+    assert us2.value == us.value  # the cached choice, not a new measurement
+    # an explicit shape forgets the cache; the next call measures again and caches anew
+    c.set_launch_shape(128, 1, 4, 1024)
+    abi.check(lib.blz_autotune_batch(c.ctx, views, len(ref), 1, None, C.byref(again), C.byref(us2)), "autotune")
+    assert again.chunkObjects in (256, 512, 1024)
+    # batches of that size run with the tuned shape and still match the oracle
+    for _, _, _, t in ref:
+        t.count.fill_(0)
+    abi.check(lib.blz_cull_batch(c.ctx, views, len(ref), None), "batch")
+    assert c.check() == 0
+    for i, (v, objs, hp, t) in enumerate(ref):
+        n, recs, _ = O.cull(3, v, sc, objects=objs, pyramid=hp)
+        assert_records_equal(t.read(), (n, recs), f"view {i} under the tuned shape {c.launch_shape()}")
+    c.set_launch_shape(256, 2)
+
+
+def test_autotune_single_caches_and_keeps_visibility(stress_ctx):
+    """blz_autotune_single times the single-view shapes on pass 2 without changing the visibility,
+    caches the fastest for (list size, pass), and pass 2 under it matches the oracle."""
+    c, sc = stress_ctx
+    v = view_for(zfar=1e4)
+    depth = O.depth_raster(v, S.make_occluders(np.random.default_rng(8), 300), W, H)
+    pyr = DevicePyramid(W, H)
+    c.generate_depth_pyramid(pyr, torch.from_numpy(depth).cuda())
+    vis0 = (np.random.default_rng(9).random(sc.count) < 0.5).astype(np.uint32)
+    vis = torch.from_numpy(vis0.view(np.int32).copy()).cuda()
+    t = Target.alloc(sc.count)
+    shape, us = c.autotune_single(v, abi.MODE_LATE, t, visibility=vis, pyramid=pyr, repeats=2)
+    assert (shape["threads"], shape["objects_per_thread"]) in SINGLE_SHAPES
+    assert shape["chunk_objects"] % 32 == 0 and shape["chunk_objects"] > 0
+    assert us > 0
+    assert np.array_equal(vis.cpu().numpy().view(np.uint32), vis0)  # the tuner worked on a copy
+    again, us2 = c.autotune_single(v, abi.MODE_LATE, t, visibility=vis, pyramid=pyr, repeats=2)
+    assert again == shape and us2 == us  # cached
+    t.count.fill_(0)
+    c.draw_cull_occlusion_pass(v, vis, pyr, t)
+    assert c.check() == 0
+    ovis = vis0.copy()
+    n, recs, _ = O.cull(2, v, sc, vis=ovis, pyramid=O.pyramid_build(depth))
+    assert_records_equal(t.read(), (n, recs), f"pass 2 under the tuned shape {shape}")
+    assert np.array_equal(vis.cpu().numpy().view(np.uint32), ovis)
+    c.set_launch_shape(256, 2)  # forgets the cached choice
+
+
+SINGLE_SHAPES = [(256, 1), (256, 2), (256, 4), (128, 2), (128, 4), (512, 1)]
 
 
 # ----------------------------------------------------------------------------- serving
