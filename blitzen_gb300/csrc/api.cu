@@ -891,13 +891,13 @@ int blz_cull_instanced(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList 
     if (nL > kMaxInstancedLods) return fail(BLZ_ERR_INVALID_ARGUMENT, "instanced cull supports up to %u LODs, scene has %u", kMaxInstancedLods, nL);
     if (nL <= kInstStagedMaxLods) {
         // the FRUSTUM decide kernel stages (object, LOD) pairs; a counting sort turns them into lists
-        const uint32_t tile = single_chunk_size(BLZ_MODE_FRUSTUM, c->singleThreads, c->singleOpt, count, c->smCount);
+        const uint32_t tile = single_chunk_size(kModeInstanced, c->singleThreads, c->singleOpt, count, c->smCount);
         uint32_t chunks = (count + tile - 1) / tile;
         if (chunks == 0) chunks = 1;
         rc = ensure_chunk_scratch(c, chunks, tile);
         if (rc != BLZ_OK) return rc;
         const uint32_t groups = instanced_group_count(chunks);
-        const size_t words = static_cast<size_t>(groups) * nL + nL + 1;  // counts, totals, finished-block counter
+        const size_t words = static_cast<size_t>(groups) * nL;  // the groups' LOD histograms
         if (words > c->instWords) {
             if (c->capturing) return fail(BLZ_ERR_CAPACITY, "scratch must grow, which a capture cannot record: run the call once before capturing");
             if (c->instScratch) {
@@ -922,6 +922,8 @@ int blz_cull_instanced(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList 
         p.chunkSize = tile;
         bind_chunk_scratch(c, p);
         p.workCounter = nullptr;
+        p.instHist = c->instScratch;
+        p.instLods = nL;
         InstStagedParams q{};
         q.staged = p.staged;
         q.chunkCount = p.chunkCount;
@@ -930,8 +932,6 @@ int blz_cull_instanced(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList 
         q.groups = groups;
         q.nL = nL;
         q.hist = c->instScratch;
-        q.totals = c->instScratch + static_cast<size_t>(groups) * nL;
-        q.done = q.totals + nL;
         q.lods = c->scene.lods;
         q.counters = counters;
         q.instances = instances;
@@ -944,7 +944,7 @@ int blz_cull_instanced(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList 
         q.status = &c->scratch->status;
         cudaError_t e = launch_instanced_staged(p, q, c->singleThreads, c->singleOpt, c->smCount, reinterpret_cast<cudaStream_t>(s));
         if (e != cudaSuccess) return cuda_fail(e, "instanced cull launch");
-        c->launches += 4;  // decide, count, offsets, place
+        c->launches += 2;  // decide (with the group histograms), place
         return BLZ_OK;
     }
     const uint32_t tiles = (count + instanced_tile_size() - 1) / instanced_tile_size();

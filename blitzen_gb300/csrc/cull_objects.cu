@@ -67,6 +67,7 @@ __device__ __forceinline__ uint32_t find_view_warp(const uint32_t* tileStart, ui
 // ------------------------------------------------------------------ decisions
 
 constexpr uint32_t kChunk = 512;  // objects per chunk of batched views (single views size theirs)
+constexpr uint32_t kInstGroup = 32;  // chunks per group of the instanced counting sort, one warp each
 
 // A frustum survivor waiting for the dense stage (32 bytes, two 16-byte shared-memory words).
 struct Survivor {
@@ -103,7 +104,7 @@ __device__ __forceinline__ void wait_pyramid(const unsigned int* ready, uint32_t
 template <int MODE>
 __device__ __forceinline__ void dense_entry(const SceneTables& sc, const BatchViewDev& bv, const ViewConsts& v, uint4 a,
                                             uint4 b, bool mine, uint2* stage, uint32_t& run, uint2* stage1 = nullptr,
-                                            uint32_t* run1 = nullptr) {
+                                            uint32_t* run1 = nullptr, uint32_t* hist = nullptr) {
     constexpr bool FUSED = fused_mode(MODE);
     constexpr bool REWRITE = MODE == BLZ_MODE_LATE || FUSED;  // pass 2's visibility rewrite
     const uint32_t obj = a.x & 0x3FFFFFFFu;  // LATE: bit 31 previous visibility != 0, bit 30 == 1
@@ -139,6 +140,11 @@ __device__ __forceinline__ void dense_entry(const SceneTables& sc, const BatchVi
     const unsigned e = __ballot_sync(0xFFFFFFFFu, emitted);
     if (emitted) stage[run + __popc(e & lanemask_lt())] = make_uint2(obj, lid);
     run += __popc(e);
+    if constexpr (MODE == kModeInstanced) {
+        // the group's histogram row (hist = row of this chunk's group): one add per distinct LOD
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, emitted ? lid : 0xFFFFFFFFu);
+        if (emitted && (peers & lanemask_lt()) == 0u) atomicAdd(hist + lid, static_cast<uint32_t>(__popc(peers)));
+    }
     if constexpr (FUSED) {
         const unsigned e1 = __ballot_sync(0xFFFFFFFFu, emitted1);
         if (emitted1) stage1[*run1 + __popc(e1 & lanemask_lt())] = make_uint2(obj, lid);
@@ -151,7 +157,8 @@ __device__ __forceinline__ void dense_entry(const SceneTables& sc, const BatchVi
 template <int MODE>
 __device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchViewDev& bv, const ViewConsts& v,
                                             const Survivor* ring, uint32_t head, uint32_t n, uint2* stage,
-                                            uint32_t& run, uint4* keep, uint32_t& kept, uint2* stage1, uint32_t* run1) {
+                                            uint32_t& run, uint4* keep, uint32_t& kept, uint2* stage1, uint32_t* run1,
+                                            uint32_t* hist = nullptr) {
     const uint32_t lane = threadIdx.x & 31u;
     const bool mine = lane < n;
     uint4 a = make_uint4(0u, 0u, 0u, 0u), b = make_uint4(0u, 0u, 0u, 0u);
@@ -165,7 +172,7 @@ __device__ __forceinline__ void dense_round(const SceneTables& sc, const BatchVi
         }
     }
     if constexpr (MODE == kModeFrame1) kept += n;
-    dense_entry<MODE>(sc, bv, v, a, b, mine, stage, run, stage1, run1);
+    dense_entry<MODE>(sc, bv, v, a, b, mine, stage, run, stage1, run1, hist);
 }
 
 // The fields of the surface table the frustum stage reads (bounding sphere; LOD offset and count),
@@ -193,7 +200,8 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
                                                     uint32_t limit, uint2* stage, Survivor* ring, uint4* cand,
                                                     const SurfaceCache& surf, unsigned int& flags, uint4* keep,
                                                     uint32_t& kept, uint2* stage1 = nullptr, uint32_t* run1 = nullptr,
-                                                    const unsigned int* ready = nullptr, uint32_t spinLimit = 0u) {
+                                                    const unsigned int* ready = nullptr, uint32_t spinLimit = 0u,
+                                                    uint32_t* hist = nullptr) {
     constexpr uint32_t STEP = 32u * OPT;
     constexpr bool PACK = (MODE == BLZ_MODE_FIRST) && SINGLE;  // candidate ring of 2 * STEP entries
     // Single-view pass 2 walks its chunk from the last object down: pass 1 walked the same chunk
@@ -223,7 +231,7 @@ __device__ __forceinline__ uint32_t decide_run_warp(const SceneTables& sc, const
             wait_pyramid(ready, spinLimit, flags);
             pyrSeen = true;
         }
-        dense_round<MODE>(sc, bv, v, ring, head, n, stage, run, keep, kept, stage1, run1);
+        dense_round<MODE>(sc, bv, v, ring, head, n, stage, run, keep, kept, stage1, run1, hist);
     };
 
     // frustum stage over OPT slices: obj[k] the object index, ro[k] its render object, vis[k] the
@@ -454,8 +462,10 @@ __device__ __forceinline__ void decide_body(const PipeParams& p, DecideSmem<MODE
                 default: total = decide_run_warp<BLZ_MODE_FRUSTUM, SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags, keep, kept); break;
             }
         } else {
+            uint32_t* hist = nullptr;
+            if constexpr (MODE == kModeInstanced) hist = p.instHist + static_cast<size_t>(chunk / kInstGroup) * p.instLods;
             total = decide_run_warp<(MODE < 0 ? 0 : MODE), SINGLE, OPT>(p.sc, bv, base, limit, stage, ring, cand, surf, flags, keep, kept,
-                                                                       stage1, &total1, ready, spinLimit);
+                                                                       stage1, &total1, ready, spinLimit, hist);
         }
         if (lane == 0) {
             p.chunkCount[chunk] = total;
@@ -894,6 +904,7 @@ uint32_t single_chunk_size(uint32_t mode, uint32_t threads, uint32_t opt, uint32
         case BLZ_MODE_FIRST: per = single_blocks_per_sm<BLZ_MODE_FIRST>(threads, opt); break;
         case BLZ_MODE_LATE: per = single_blocks_per_sm<BLZ_MODE_LATE>(threads, opt); break;
         case BLZ_MODE_TEMPORAL: per = single_blocks_per_sm<BLZ_MODE_TEMPORAL>(threads, opt); break;
+        case kModeInstanced: per = single_blocks_per_sm<kModeInstanced>(threads, opt); break;
         default: per = single_blocks_per_sm<BLZ_MODE_FRUSTUM>(threads, opt); break;
     }
     const uint64_t warps = static_cast<uint64_t>(per) * static_cast<uint64_t>(smCount > 0 ? smCount : 1) * (threads / 32u);
@@ -934,146 +945,37 @@ cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t thre
 // ------------------------------------------------------------------ instanced cull from the staged records
 //
 // The instanced cull (drawInstCountReset + drawInstCull + drawInstCmd) decides exactly what the
-// frustum + LOD pass decides: every visible object and its LOD. So it runs the FRUSTUM decide
-// kernel, whose staged (objectId, lodId) records are in object order per chunk, and then turns
-// them into per-LOD instance lists with a stable counting sort over groups of kInstGroup chunks.
-// The group counts are kept LOD-major (hist[lod * groups + group]) so that one LOD's counts are
-// contiguous:
-//   count    per group, the number of records of each LOD (shared-memory histogram);
-//   offsets  one warp per LOD loads all of that LOD's group counts at once, scans them into
-//            exclusive offsets and writes the LOD's total; the block that finishes last writes the
-//            counters and, in ascending LOD order, one command per non-empty LOD;
-//   place    per group, the group's offset in each LOD's list and the LODs' instanceOffsets are
-//            staged in shared memory while each warp counts its chunk's records per LOD; the block scans those rows
-//            per LOD, and each warp places its records in order (ranks inside 32-record slices
-//            from __match_any_sync).
-
-constexpr uint32_t kInstGroup = 32;  // chunks per group, one warp each
-constexpr uint32_t kInstOffPer = 4;  // group counts per lane per round of the offsets scan
-
-__global__ void __launch_bounds__(kInstGroup * 32) inst_count_kernel(const InstStagedParams q) {
-    extern __shared__ uint32_t s_hist[];  // [nL]
-    const uint32_t nL = q.nL;
-    for (uint32_t b = threadIdx.x; b < nL; b += kInstGroup * 32) s_hist[b] = 0u;
-    __syncthreads();
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t chunk = blockIdx.x * kInstGroup + warp;
-    if (chunk < q.totalTiles) {
-        const uint32_t n = __ldcg(q.chunkCount + chunk);
-        const uint2* st = q.staged + static_cast<size_t>(chunk) * q.chunkSize;
-        for (uint32_t j = lane; j < n; j += 32) atomicAdd(&s_hist[__ldcg(st + j).y], 1u);
-    }
-    __syncthreads();
-    for (uint32_t b = threadIdx.x; b < nL; b += kInstGroup * 32) q.hist[static_cast<size_t>(b) * q.groups + blockIdx.x] = s_hist[b];
-    if (blockIdx.x == 0 && threadIdx.x == 0) *q.done = 0u;  // the offsets launch's finished-block counter
-}
-
-__global__ void __launch_bounds__(1024) inst_offsets_kernel(const InstStagedParams q) {
-    __shared__ uint32_t s_warpSums[32];
-    __shared__ uint32_t s_last;
-    __shared__ unsigned int s_flags;
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t b = blockIdx.x * 32u + warp;
-    if (b < q.nL) {
-        uint32_t* h = q.hist + static_cast<size_t>(b) * q.groups;
-        uint32_t run = 0;
-        for (uint32_t g0 = 0; g0 < q.groups; g0 += 32u * kInstOffPer) {
-            // lane L holds groups g0 + L*kInstOffPer .. +kInstOffPer-1 (all loads issued together)
-            uint32_t x[kInstOffPer];
-            uint32_t mine = 0;
-#pragma unroll
-            for (uint32_t k = 0; k < kInstOffPer; ++k) {
-                const uint32_t g = g0 + lane * kInstOffPer + k;
-                x[k] = g < q.groups ? __ldcg(h + g) : 0u;
-                mine += x[k];
-            }
-            uint32_t incl = mine;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                if (lane >= static_cast<uint32_t>(o)) incl += n;
-            }
-            uint32_t at = run + incl - mine;
-#pragma unroll
-            for (uint32_t k = 0; k < kInstOffPer; ++k) {
-                const uint32_t g = g0 + lane * kInstOffPer + k;
-                if (g < q.groups) h[g] = at;
-                at += x[k];
-            }
-            run += __shfl_sync(0xFFFFFFFFu, incl, 31);
-        }
-        if (lane == 0) q.totals[b] = run;
-    }
-    // the block that finishes last (threadfence reduction: a counter, no waiting) writes the
-    // counters and, in ascending LOD order, one command per non-empty LOD
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        s_last = atomicAdd(q.done, 1u) == gridDim.x - 1u ? 1u : 0u;
-        s_flags = 0u;
-    }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    const uint32_t nL = q.nL;
-    const uint32_t slots = q.slotsPerLod ? q.slotsPerLod : 0xFFFFFFFFu;
-    const uint32_t per = (nL + 1023u) / 1024u;
-    const uint32_t b0 = min(nL, threadIdx.x * per), b1 = min(nL, b0 + per);
-    uint32_t mine = 0;
-    for (uint32_t l = b0; l < b1; ++l) mine += __ldcg(q.totals + l) ? 1u : 0u;
-    uint32_t incl = mine;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= static_cast<uint32_t>(o)) incl += x;
-    }
-    if (lane == 31) s_warpSums[warp] = incl;
-    __syncthreads();
-    uint32_t warpOff = 0, all = 0;
-    for (uint32_t w = 0; w < 32u; ++w) {
-        if (w < warp) warpOff += s_warpSums[w];
-        all += s_warpSums[w];
-    }
-    uint32_t out = warpOff + incl - mine;
-    unsigned int f = 0u;
-    for (uint32_t l = b0; l < b1; ++l) {
-        const uint32_t total = __ldcg(q.totals + l);
-        q.counters[l].instanceCount = total;
-        const uint32_t offset = __ldg(&q.counters[l].instanceOffset);
-        if (total > slots || static_cast<uint64_t>(offset) + min(total, slots) > q.instanceCapacity)
-            f |= BLZ_FLAG_INSTANCE_OVERFLOW;
-        if (total == 0u) continue;
-        if (out < q.capacity) {
-            uint32_t* w = reinterpret_cast<uint32_t*>(q.cmds + static_cast<size_t>(out) * q.stride);
-            const uint2 lod = __ldg(reinterpret_cast<const uint2*>(q.lods + l));  // indexCount, firstIndex
-            w[0] = offset;
-            w[1] = lod.x;
-            w[2] = min(total, slots);
-            w[3] = lod.y;
-            w[4] = 0u;
-            w[5] = 0u;
-        }
-        ++out;
-    }
-    if (all > q.capacity) f |= BLZ_FLAG_COMMAND_OVERFLOW;
-    if (f) atomicOr(&s_flags, f);
-    if (threadIdx.x == 0) *q.drawCount = all;
-    __syncthreads();
-    if (threadIdx.x == 0 && s_flags) atomicOr(q.status, s_flags);
-}
+// frustum + LOD pass decides: every visible object and its LOD. So it runs that decide kernel
+// (kModeInstanced), whose staged (objectId, lodId) records are in object order per chunk and which
+// also counts each group's records per LOD (hist[group][lod], groups of kInstGroup chunks, zeroed
+// before the launch), and then one place launch, a block per group:
+//   offsets  each LOD's offset for the group is the sum of the LOD's counts in the groups before it
+//            (coalesced loads across LODs, the block's threads taking interleaved groups); block 0,
+//            which has no group before it, sums all of them instead, which gives every LOD's total,
+//            and writes the counters and, in ascending LOD order, one command per non-empty LOD;
+//   rows     each warp counts its chunk's records per LOD, and the block scans those rows per LOD;
+//   place    each warp places its records in order (ranks inside 32-record slices from
+//            __match_any_sync).
 
 constexpr uint32_t kInstBatch = 4;  // 32-record slices whose loads are issued together
+constexpr uint32_t kInstThreads = kInstGroup * 32;
 
-__global__ void __launch_bounds__(kInstGroup * 32) inst_place_kernel(const InstStagedParams q) {
+__global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStagedParams q) {
     // [kInstGroup][nL] per-warp counts, then offsets; [nL] the group's offset in each LOD's list;
-    // [nL] each LOD's instanceOffset
+    // [nL] each LOD's instanceOffset; [nL] (block 0) each LOD's total; [R][nL] partial sums
     extern __shared__ uint32_t s_rows[];
     __shared__ unsigned int s_flags;
-    const uint32_t nL = q.nL;
+    __shared__ uint32_t s_warpSums[32];
+    const uint32_t nL = q.nL, G = q.groups, g = blockIdx.x;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     uint32_t* s_goff = s_rows + kInstGroup * nL;
     uint32_t* s_ioff = s_goff + nL;
-    const uint32_t chunk = blockIdx.x * kInstGroup + warp;
+    uint32_t* s_tot = s_ioff + nL;
+    uint32_t* s_part = s_tot + nL;
+    // thread t works on LOD t % nL as row t / nL of R rows (nL <= kInstStagedMaxLods <= kInstThreads)
+    const uint32_t R = kInstThreads / nL;
+    const uint32_t tb = threadIdx.x % nL, tr = threadIdx.x / nL;
+    const uint32_t chunk = g * kInstGroup + warp;
     const uint32_t n = chunk < q.totalTiles ? __ldcg(q.chunkCount + chunk) : 0u;
     const uint2* st = q.staged + static_cast<size_t>(chunk) * q.chunkSize;
     auto load_batch = [&](uint32_t j0, uint2 (&r)[kInstBatch]) {
@@ -1085,13 +987,30 @@ __global__ void __launch_bounds__(kInstGroup * 32) inst_place_kernel(const InstS
     };
     uint2 first[kInstBatch];  // the chunk's first 128 records, loaded once for both walks
     load_batch(0, first);
-    for (uint32_t b = threadIdx.x; b < nL; b += kInstGroup * 32) {
-        s_goff[b] = __ldcg(q.hist + static_cast<size_t>(b) * q.groups + blockIdx.x);
+    for (uint32_t b = threadIdx.x; b < nL; b += kInstThreads) {
+        s_goff[b] = 0u;
+        s_tot[b] = 0u;
         s_ioff[b] = __ldg(&q.counters[b].instanceOffset);
     }
-    for (uint32_t j = threadIdx.x; j < kInstGroup * nL; j += kInstGroup * 32) s_rows[j] = 0u;
+    for (uint32_t j = threadIdx.x; j < kInstGroup * nL; j += kInstThreads) s_rows[j] = 0u;
     if (threadIdx.x == 0) s_flags = 0u;
     __syncthreads();
+    // 0. the group's offset in each LOD's list: the LOD's counts of the groups before this one,
+    //    row tr taking every R-th group (coalesced across LODs). Block 0, which has none before
+    //    it, sums every group instead: each LOD's total, for the commands (step 4).
+    if (tr < R) {
+        const uint32_t g1 = g == 0 ? G : g;
+        uint32_t sum = 0, gg = tr;
+        for (; gg + 7u * R < g1; gg += 8u * R) {  // eight loads in flight at a time
+            uint32_t x[8];
+#pragma unroll
+            for (uint32_t k = 0; k < 8u; ++k) x[k] = __ldcg(q.hist + static_cast<size_t>(gg + k * R) * nL + tb);
+#pragma unroll
+            for (uint32_t k = 0; k < 8u; ++k) sum += x[k];
+        }
+        for (; gg < g1; gg += R) sum += __ldcg(q.hist + static_cast<size_t>(gg) * nL + tb);
+        if (sum) atomicAdd(g == 0 ? &s_tot[tb] : &s_goff[tb], sum);
+    }
     uint32_t* row = s_rows + warp * nL;
     const uint32_t lt = lanemask_lt();
     // 1. this chunk's records per LOD (only this warp touches its row)
@@ -1112,12 +1031,23 @@ __global__ void __launch_bounds__(kInstGroup * 32) inst_place_kernel(const InstS
         }
     }
     __syncthreads();
-    // 2. per LOD, exclusive offsets of the warps' chunks inside the group
-    for (uint32_t b = threadIdx.x; b < nL; b += kInstGroup * 32) {
+    // 2. per LOD, exclusive offsets of the warps' chunks inside the group: row tr of threads sums
+    //    its kInstGroup / R consecutive warps' counts, then scans them after the sums of the rows
+    //    before it
+    const uint32_t per = (kInstGroup + R - 1u) / R;
+    const uint32_t w0 = min(kInstGroup, tr * per), w1 = min(kInstGroup, w0 + per);
+    if (tr < R) {
+        uint32_t part = 0;
+        for (uint32_t w = w0; w < w1; ++w) part += s_rows[w * nL + tb];
+        s_part[tr * nL + tb] = part;
+    }
+    __syncthreads();
+    if (tr < R) {
         uint32_t run = 0;
-        for (uint32_t w = 0; w < kInstGroup; ++w) {
-            const uint32_t c = s_rows[w * nL + b];
-            s_rows[w * nL + b] = run;
+        for (uint32_t r = 0; r < tr; ++r) run += s_part[r * nL + tb];
+        for (uint32_t w = w0; w < w1; ++w) {
+            const uint32_t c = s_rows[w * nL + tb];
+            s_rows[w * nL + tb] = run;
             run += c;
         }
     }
@@ -1150,6 +1080,49 @@ __global__ void __launch_bounds__(kInstGroup * 32) inst_place_kernel(const InstS
             __syncwarp();
         }
     }
+    // 4. block 0: the counters and, in ascending LOD order, one command per non-empty LOD
+    //    (drawInstCmd.cs.hlsl:9-38)
+    if (g == 0) {
+        const uint32_t perT = (nL + kInstThreads - 1u) / kInstThreads;
+        const uint32_t b0 = min(nL, threadIdx.x * perT), b1 = min(nL, b0 + perT);
+        uint32_t mine = 0;
+        for (uint32_t l = b0; l < b1; ++l) mine += s_tot[l] ? 1u : 0u;
+        uint32_t incl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= static_cast<uint32_t>(o)) incl += x;
+        }
+        if (lane == 31) s_warpSums[warp] = incl;
+        __syncthreads();
+        uint32_t warpOff = 0, all = 0;
+        for (uint32_t w = 0; w < 32u; ++w) {
+            if (w < warp) warpOff += s_warpSums[w];
+            all += s_warpSums[w];
+        }
+        uint32_t out = warpOff + incl - mine;
+        for (uint32_t l = b0; l < b1; ++l) {
+            const uint32_t total = s_tot[l];
+            q.counters[l].instanceCount = total;
+            const uint32_t offset = s_ioff[l];
+            if (total > slots || static_cast<uint64_t>(offset) + min(total, slots) > q.instanceCapacity)
+                flags |= BLZ_FLAG_INSTANCE_OVERFLOW;
+            if (total == 0u) continue;
+            if (out < q.capacity) {
+                uint32_t* w = reinterpret_cast<uint32_t*>(q.cmds + static_cast<size_t>(out) * q.stride);
+                const uint2 lod = __ldg(reinterpret_cast<const uint2*>(q.lods + l));  // indexCount, firstIndex
+                w[0] = offset;
+                w[1] = lod.x;
+                w[2] = min(total, slots);
+                w[3] = lod.y;
+                w[4] = 0u;
+                w[5] = 0u;
+            }
+            ++out;
+        }
+        if (all > q.capacity) flags |= BLZ_FLAG_COMMAND_OVERFLOW;
+        if (threadIdx.x == 0) *q.drawCount = all;
+    }
     if (flags) atomicOr(&s_flags, flags);
     __syncthreads();
     if (threadIdx.x == 0 && s_flags) atomicOr(q.status, s_flags);
@@ -1159,23 +1132,21 @@ uint32_t instanced_group_count(uint32_t chunks) { return (chunks + kInstGroup - 
 
 cudaError_t launch_instanced_staged(const PipeParams& p, const InstStagedParams& q, uint32_t threads, uint32_t opt,
                                     int smCount, cudaStream_t s) {
-    cudaError_t e;
-    if (threads == 256 && opt == 1) e = launch_decide_t<BLZ_MODE_FRUSTUM, true, 256, 1>(p, 0, smCount, s);
-    else if (threads == 256 && opt == 4) e = launch_decide_t<BLZ_MODE_FRUSTUM, true, 256, 4>(p, 0, smCount, s);
-    else if (threads == 128 && opt == 2) e = launch_decide_t<BLZ_MODE_FRUSTUM, true, 128, 2>(p, 0, smCount, s);
-    else if (threads == 128 && opt == 4) e = launch_decide_t<BLZ_MODE_FRUSTUM, true, 128, 4>(p, 0, smCount, s);
-    else if (threads == 512 && opt == 1) e = launch_decide_t<BLZ_MODE_FRUSTUM, true, 512, 1>(p, 0, smCount, s);
-    else e = launch_decide_t<BLZ_MODE_FRUSTUM, true, kObjThreads, kObjOpt>(p, 0, smCount, s);
+    cudaError_t e = cudaMemsetAsync(p.instHist, 0, sizeof(uint32_t) * static_cast<size_t>(q.groups) * q.nL, s);
     if (e != cudaSuccess) return e;
-    const size_t histBytes = sizeof(uint32_t) * q.nL;
-    const size_t rowBytes = sizeof(uint32_t) * (kInstGroup + 2) * q.nL;
+    if (threads == 256 && opt == 1) e = launch_decide_t<kModeInstanced, true, 256, 1>(p, 0, smCount, s);
+    else if (threads == 256 && opt == 4) e = launch_decide_t<kModeInstanced, true, 256, 4>(p, 0, smCount, s);
+    else if (threads == 128 && opt == 2) e = launch_decide_t<kModeInstanced, true, 128, 2>(p, 0, smCount, s);
+    else if (threads == 128 && opt == 4) e = launch_decide_t<kModeInstanced, true, 128, 4>(p, 0, smCount, s);
+    else if (threads == 512 && opt == 1) e = launch_decide_t<kModeInstanced, true, 512, 1>(p, 0, smCount, s);
+    else e = launch_decide_t<kModeInstanced, true, kObjThreads, kObjOpt>(p, 0, smCount, s);
+    if (e != cudaSuccess) return e;
+    const size_t rowBytes = sizeof(uint32_t) * ((kInstGroup + 3) * q.nL + (kInstThreads / q.nL) * q.nL);
     if (rowBytes > 48 * 1024) {
         e = cudaFuncSetAttribute(inst_place_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(rowBytes));
         if (e != cudaSuccess) return e;
     }
-    inst_count_kernel<<<q.groups, kInstGroup * 32, histBytes, s>>>(q);
-    inst_offsets_kernel<<<(q.nL + 31) / 32, 1024, 0, s>>>(q);
-    inst_place_kernel<<<q.groups, kInstGroup * 32, rowBytes, s>>>(q);
+    inst_place_kernel<<<q.groups, kInstThreads, rowBytes, s>>>(q);
     return cudaGetLastError();
 }
 

@@ -66,6 +66,10 @@ constexpr int kModeFrameFused = 5;
 // buffer): the kernel's blocks first build the pyramid's tiles, taken by ticket, and a warp waits
 // for the finished pyramid (a flag in the context's scratch) before its first Hi-Z test.
 constexpr int kModeFramePyr = 6;
+// The frustum + LOD pass of the instanced cull: BLZ_MODE_FRUSTUM, and every emitted record also
+// counts towards its group's LOD histogram (PipeParams.instHist: [group][LOD], 32 chunks a group),
+// which the place kernel turns into list offsets.
+constexpr int kModeInstanced = 7;
 
 constexpr int kObjThreads = 256;
 constexpr int kObjOpt = 2;
@@ -111,6 +115,9 @@ struct PipeParams {
     uint32_t* keepCount;   // kept frame: [totalTiles] survivors per chunk
     uint2* staged2;        // fused frame: pass 1's staged records, [totalTiles * chunkSize]
     uint32_t* chunkCount2; // fused frame: [totalTiles]
+    uint32_t* instHist;    // instanced pass: [groups][lodCount] record counts (zero before the launch)
+    uint32_t instLods;     // instanced pass: the histogram's row length (the scene's LOD count)
+    uint32_t pad2;
 };
 
 struct InstancedParams {
@@ -138,9 +145,7 @@ struct InstStagedParams {
     const uint32_t* chunkCount; // [totalTiles]
     uint32_t totalTiles, chunkSize;
     uint32_t groups, nL;        // chunk groups of the counting sort, LOD count
-    uint32_t* hist;             // scratch [groups * nL]: group counts, then exclusive offsets
-    uint32_t* totals;           // scratch [nL]
-    uint32_t* done;             // scratch: offsets blocks that finished
+    const uint32_t* hist;       // [groups][nL] record counts per group and LOD (the decide kernel's)
     const BlzLodData* lods;
     BlzLodInstanceCounter* counters;
     uint32_t* instances;
@@ -237,7 +242,7 @@ bool batch_shape_supported(uint32_t threads, uint32_t opt);
 cudaError_t launch_batch_cull(const PipeParams& p, uint32_t threads, uint32_t opt, uint32_t blocksPerSm, int smCount,
                               cudaStream_t s, int mode);
 uint32_t instanced_tile_size();
-constexpr uint32_t kInstStagedMaxLods = 1024;  // the staged instanced path keeps [34][LODs] words in shared memory
+constexpr uint32_t kInstStagedMaxLods = 1024;  // the staged instanced path keeps [36 to 39][LODs] words in shared memory
 uint32_t instanced_group_count(uint32_t chunks);
 cudaError_t launch_instanced_staged(const PipeParams& p, const InstStagedParams& q, uint32_t threads, uint32_t opt,
                                     int smCount, cudaStream_t s);
