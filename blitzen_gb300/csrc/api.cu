@@ -110,23 +110,24 @@ int ensure_chunk_scratch(blz_ctx* c, size_t chunks, size_t chunkSize) {
     return BLZ_OK;
 }
 
-// Cluster-cull scratch for `tiles` tiles: counts and their exclusive prefix per tile (uint2),
-// candidates per tile, the
-// objects' cluster ranges, transforms and survivor counts, then the visibility bits (bitWords per
-// tile). Grown on demand like the
-// object-cull scratch.
+// Cluster-cull scratch for `tiles` tiles. First the work list's item count (zero between launches:
+// zeroed when allocated, rewound by the emit launch) and the frame's totals. Then, laid out for this
+// call's tile count: counts per tile (uint2), candidates per tile, the objects' cluster ranges, transforms and survivor counts, the
+// work list, and the visibility bits (bitWords per tile). Grown on demand like the object-cull
+// scratch.
 int bind_cluster_scratch(blz_ctx* c, uint32_t tiles, ClusterParams& p) {
     const size_t objs = static_cast<size_t>(tiles) * cluster_tile_objects();
     const uint32_t bitWords = std::max<uint32_t>(c->lodClusterMax, 1u);  // 32 objects x max clusters / 32 bits
-    const uint32_t split = cluster_split(c->lodClusterMax);
     auto r256 = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t headBytes = 256;
     const size_t countBytes = r256(static_cast<size_t>(tiles) * sizeof(uint2));
     const size_t tileBytes = r256(static_cast<size_t>(tiles) * sizeof(uint32_t));
     const size_t infoBytes = r256(objs * sizeof(uint2));
     const size_t xfBytes = r256(objs * 2 * sizeof(float4));
     const size_t survBytes = r256(objs * sizeof(uint32_t));
+    const size_t itemBytes = r256(static_cast<size_t>(cluster_max_items(tiles, bitWords)) * sizeof(uint4));
     const size_t bitBytes = static_cast<size_t>(tiles) * bitWords * sizeof(uint32_t);
-    const size_t need = 2 * countBytes + tileBytes + infoBytes + xfBytes + survBytes + bitBytes;
+    const size_t need = headBytes + countBytes + tileBytes + infoBytes + xfBytes + survBytes + itemBytes + bitBytes;
     if (need > c->clusterBytes) {
         if (c->capturing) return fail(BLZ_ERR_CAPACITY, "scratch must grow, which a capture cannot record: run the call once before capturing");
         if (c->clusterMem) {
@@ -138,12 +139,19 @@ int bind_cluster_scratch(blz_ctx* c, uint32_t tiles, ClusterParams& p) {
         const size_t want = need + need / 4;
         if (cudaMalloc(&c->clusterMem, want) != cudaSuccess)
             return fail(BLZ_ERR_OUT_OF_MEMORY, "cluster-cull scratch of %zu bytes", want);
+        const cudaError_t e = cudaMemset(c->clusterMem, 0, headBytes);  // the work list's counts start at zero
+        if (e != cudaSuccess) {
+            cudaFree(c->clusterMem);
+            c->clusterMem = nullptr;
+            return cuda_fail(e, "zeroing the cluster-cull scratch");
+        }
         c->clusterBytes = want;
     }
     char* m = static_cast<char*>(c->clusterMem);
+    p.itemCount = reinterpret_cast<uint32_t*>(m);
+    p.totals = reinterpret_cast<uint2*>(m + 8);
+    m += headBytes;
     p.tileCount = reinterpret_cast<uint32_t*>(m);
-    m += countBytes;
-    p.tilePrefix = reinterpret_cast<uint2*>(m);
     m += countBytes;
     p.tileSlots = reinterpret_cast<uint32_t*>(m);
     m += tileBytes;
@@ -153,10 +161,12 @@ int bind_cluster_scratch(blz_ctx* c, uint32_t tiles, ClusterParams& p) {
     m += xfBytes;
     p.objSurv = reinterpret_cast<uint32_t*>(m);
     m += survBytes;
+    p.items = reinterpret_cast<uint4*>(m);
+    m += itemBytes;
     p.bits = reinterpret_cast<uint32_t*>(m);
     p.bitWords = bitWords;
     p.tiles = tiles;
-    p.split = split;
+    p.smCount = static_cast<uint32_t>(c->smCount);
     return BLZ_OK;
 }
 
@@ -1000,7 +1010,7 @@ int blz_cull_clusters(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList l
     p.scratch = c->scratch;
     cudaError_t e = launch_cluster_cull(p, *view, reinterpret_cast<cudaStream_t>(s));
     if (e != cudaSuccess) return cuda_fail(e, "cluster cull launch");
-    c->launches += 4;  // objects, tests, scan, emit
+    c->launches += 3;  // objects, tests, emit
     return BLZ_OK;
 }
 
@@ -1040,7 +1050,7 @@ int blz_cull_cluster_tasks(blz_ctx* c, const BlzCameraViewData* view, BlzRenderL
     p.payloadCount = target->payloadCount;
     cudaError_t e = launch_cluster_tasks(p, *view, reinterpret_cast<cudaStream_t>(s));
     if (e != cudaSuccess) return cuda_fail(e, "cluster task cull launch");
-    c->launches += 5;  // objects, tests, task totals, scan, emit
+    c->launches += 3;  // objects, tests, emit
     return BLZ_OK;
 }
 

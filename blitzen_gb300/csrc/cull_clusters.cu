@@ -3,20 +3,26 @@
 // The reference splits this into PreClusterDrawCull.comp.glsl:13-47 (object frustum + LOD, then a
 // serial loop that materialises one 12-byte ClusterDispatchData per cluster), a fence wait and CPU
 // read-back of the cluster count (src/Renderer/BlitzenVulkan/vulkanDraw.cpp:874-905), and
-// InitialClusterCull.comp.glsl:12-55 (one draw per cluster, its cone test commented out). Here a
-// block takes a tile of 32 objects, decides them and prefix-sums their cluster counts in shared
-// memory, then walks the tile's clusters in order (a binary search maps a cluster slot back to
-// its object), testing each one: sphere frustum, Hi-Z when a pyramid is bound, and the normal cone
-// in meshoptimizer's documented form (VendorCode/Meshoptimizer/meshoptimizer.h:561-569).
-// Two launches, no block waiting on another. The test launch keeps one visibility bit per
-// candidate cluster, each object's cluster range and the tile's survivor count; the emit launch
-// sums the counts of the tiles before its own (a strided read) and writes a record for every set
-// bit at its final position, without repeating a test. Nothing is materialised per candidate but
-// the bit, and the host never waits.
+// InitialClusterCull.comp.glsl:12-55 (one draw per cluster, its cone test commented out). Here,
+// three launches with no block waiting on another and no host wait:
+//   objects  one warp per tile of 32 objects: frustum + LOD select; the chosen LODs' clusters are
+//            numbered object by object inside the tile (slots), and each object's clusters join a
+//            work list in items of up to 64;
+//   test     a persistent grid of warps, one item at a time: every cluster of the item is tested,
+//            sphere frustum, Hi-Z when a pyramid is bound, and the normal cone in meshoptimizer's
+//            documented form (VendorCode/Meshoptimizer/meshoptimizer.h:561-569). A visible cluster
+//            sets its bit in the tile's slot-ordered visibility words and counts towards its tile
+//            and the frame;
+//   emit     one warp per tile with records: the records of the tiles before it (a strided sum of
+//            their counts), then a record for every set bit at its final position, without
+//            repeating a test.
+// Nothing is materialised per candidate cluster but its bit.
 //
-// The task form (mesh-shader consumers) runs the same tests; its test launch also keeps each
-// object's number of survivors, from which the emit launch places the object's task record and
-// its run of 32-meshlet payloads (MeshTaskPayload, VulkanShaderHeaders/ShaderBuffers.glsl:203-206).
+// The task form (mesh-shader consumers) runs the same tests; its test launch also counts each
+// object's survivors, from which the emit launch places the object's task record and its run of
+// 32-meshlet payloads (MeshTaskPayload, VulkanShaderHeaders/ShaderBuffers.glsl:203-206).
+#include <algorithm>
+
 #include "blz_device.cuh"
 #include "kernels.h"
 
@@ -25,7 +31,8 @@ namespace blz {
 constexpr int kClThreads = 256;
 constexpr int kClWarps = kClThreads / 32;
 constexpr uint32_t kClObjects = 32;  // objects per tile
-constexpr uint32_t kClMaxSplit = 4;  // test blocks per tile, at most
+constexpr uint32_t kClItem = 64;     // clusters per work item of the test launch (two per lane)
+constexpr uint32_t kClPrefixLoads = 16;  // emit launch: tile counts each lane loads at once
 
 // Sphere, Hi-Z and cone tests of one cluster of an object. The int8 cone axis and cutoff are divided
 // by 127 only for the clusters that reach the cone test (about 2 % of them behind the occluders of a
@@ -34,7 +41,6 @@ __device__ __forceinline__ bool cluster_visible(const ClusterParams& p, const Vi
                                                 const float4 quat, uint32_t cid) {
     const float4* cp = reinterpret_cast<const float4*>(p.sc.clusters + cid);
     const float4 sph = __ldg(cp);
-    const uint32_t cone = __ldg(reinterpret_cast<const uint32_t*>(cp + 1));  // int8 axis xyz, cutoff
     const Vec3 w = model_to_world(Vec3{sph.x, sph.y, sph.z}, posScale, quat);
     const Vec3 c = view_transform(v.rows, w);
     const float r = BLZ_FM(sph.w, posScale.w);
@@ -44,6 +50,7 @@ __device__ __forceinline__ bool cluster_visible(const ClusterParams& p, const Vi
         if (project_sphere(c, r, v.zNear, v.proj0, v.proj5, aabb)) vis = vis && occlusion(aabb, p.pyr, v, c, r);
     }
     if (vis) {
+        const uint32_t cone = __ldg(reinterpret_cast<const uint32_t*>(cp + 1));  // int8 axis xyz, cutoff
         const int ax = static_cast<int8_t>(cone & 0xFFu), ay = static_cast<int8_t>((cone >> 8) & 0xFFu);
         const int az = static_cast<int8_t>((cone >> 16) & 0xFFu), ac = static_cast<int8_t>(cone >> 24);
         const Vec3 axm{BLZ_FD(static_cast<float>(ax), 127.0f), BLZ_FD(static_cast<float>(ay), 127.0f),
@@ -75,20 +82,11 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t w, uint32_t n) {
     return pos;
 }
 
-// Last object of the tile whose first slot is <= slot.
-__device__ __forceinline__ uint32_t slot_object(const uint32_t* s_start, uint32_t slot) {
-    uint32_t lo = 0, hi = kClObjects;
-    while (hi - lo > 1u) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (s_start[mid] <= slot) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
 // Object launch, one warp per tile of 32 objects: frustum + LOD select (PreClusterDrawCull.comp.glsl:
 // 20-37). Keeps each object's cluster range and transform and the tile's number of candidate
-// clusters for the test launch.
+// clusters (slots, numbered object by object) for the later launches, zeroes the tile's visibility
+// words, survivor counts and tile counts, and appends the object's clusters to the work list as
+// items of up to kClItem clusters {object, first cluster, first slot in the tile, clusters}.
 template <bool TASKS>
 __global__ void __launch_bounds__(kClThreads) cluster_object_kernel(const ClusterParams p, const BlzCameraViewData view) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -123,7 +121,9 @@ __global__ void __launch_bounds__(kClThreads) cluster_object_kernel(const Cluste
                     if (__ldg(&p.sc.lods[sm.y + k].error) < threshold) idx = k;
                 const uint4 lod = __ldg(reinterpret_cast<const uint4*>(p.sc.lods + sm.y + idx));
                 // lod.z = clusterOffset, lod.w = clusterCount
-                if (lod.z > p.sc.clusterCount || lod.w > p.sc.clusterCount - lod.z) {
+                if (lod.z > p.sc.clusterCount || lod.w > p.sc.clusterCount - lod.z || lod.w > p.bitWords) {
+                    // (a range longer than the longest the scene had at upload does not fit the
+                    // tile's visibility words or the work list: the object emits nothing)
                     flags |= BLZ_FLAG_BAD_INDEX;
                 } else {
                     clusterOffset = lod.z;
@@ -132,19 +132,34 @@ __global__ void __launch_bounds__(kClThreads) cluster_object_kernel(const Cluste
             }
         }
     }
-    uint32_t total = __reduce_add_sync(0xFFFFFFFFu, count);
-    if (total > 32u * p.bitWords) {
-        // a LOD's cluster range grew past the largest one the scene had at upload: the tile's
-        // bits would not fit, so it emits nothing and flags the scene
-        flags |= BLZ_FLAG_BAD_INDEX;
-        count = 0u;
-        total = 0u;
+    uint32_t incl = count;
+    const uint32_t nItems = (count + kClItem - 1u) / kClItem;
+    uint32_t itemIncl = nItems;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        const uint32_t m = __shfl_up_sync(0xFFFFFFFFu, itemIncl, d);
+        if (lane >= static_cast<uint32_t>(d)) {
+            incl += n;
+            itemIncl += m;
+        }
     }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    const uint32_t itemTotal = __shfl_sync(0xFFFFFFFFu, itemIncl, 31);
+    uint32_t itemBase = 0;
+    if (lane == 31 && itemTotal != 0u) itemBase = atomicAdd(p.itemCount, itemTotal);
+    itemBase = __shfl_sync(0xFFFFFFFFu, itemBase, 31) + itemIncl - nItems;
+    const uint32_t start = incl - count;  // the object's first slot
+    for (uint32_t q = 0; q < nItems; ++q)
+        p.items[itemBase + q] = make_uint4(i, clusterOffset + q * kClItem, start + q * kClItem, min(kClItem, count - q * kClItem));
+    uint32_t* bits = p.bits + static_cast<size_t>(tile) * p.bitWords;
+    for (uint32_t w = lane; w < (total + 31u) / 32u; w += 32u) bits[w] = 0u;
     p.objInfo[i] = make_uint2(clusterOffset, count);
-    if constexpr (TASKS) p.objSurv[i] = 0u;
+    p.objSurv[i] = 0u;
     p.objXf[2u * i] = posScale;
     p.objXf[2u * i + 1u] = quat;
     flags = __reduce_or_sync(0xFFFFFFFFu, flags);
+    if (tile == 0u && lane == 0) *p.totals = make_uint2(0u, 0u);
     if (lane == 0) {
         p.tileSlots[tile] = total;
         reinterpret_cast<uint2*>(p.tileCount)[tile] = make_uint2(0u, 0u);
@@ -152,164 +167,67 @@ __global__ void __launch_bounds__(kClThreads) cluster_object_kernel(const Cluste
     }
 }
 
-constexpr int kScanThreads = 1024;
-
-// Scan launch, one block: exclusive prefix of the tiles' {records, 0} (task form: {tasks,
-// payloads}) counts, tileCount -> tilePrefix.
-__global__ void __launch_bounds__(kScanThreads) cluster_scan_kernel(const ClusterParams p) {
-    __shared__ uint32_t s_a[kScanThreads / 32];
-    __shared__ uint32_t s_b[kScanThreads / 32];
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint2* tc = reinterpret_cast<const uint2*>(p.tileCount);
-    constexpr uint32_t kPer = 2;  // tiles per thread per round
-    uint32_t carryA = 0, carryB = 0;
-    for (uint32_t base = 0; base < p.tiles; base += kScanThreads * kPer) {
-        const uint32_t t0 = base + threadIdx.x * kPer;
-        uint2 v[kPer];
-        uint32_t a = 0, b = 0;
-#pragma unroll
-        for (uint32_t j = 0; j < kPer; ++j) {
-            v[j] = t0 + j < p.tiles ? __ldcg(tc + t0 + j) : make_uint2(0u, 0u);
-            a += v[j].x;
-            b += v[j].y;
-        }
-        uint32_t ia = a, ib = b;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t na = __shfl_up_sync(0xFFFFFFFFu, ia, d);
-            const uint32_t nb = __shfl_up_sync(0xFFFFFFFFu, ib, d);
-            if (lane >= static_cast<uint32_t>(d)) {
-                ia += na;
-                ib += nb;
-            }
-        }
-        if (lane == 31) {
-            s_a[warp] = ia;
-            s_b[warp] = ib;
-        }
-        __syncthreads();
-        if (warp == 0) {  // scan of the warp totals
-            uint32_t wa = s_a[lane], wb = s_b[lane];
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t na = __shfl_up_sync(0xFFFFFFFFu, wa, d);
-                const uint32_t nb = __shfl_up_sync(0xFFFFFFFFu, wb, d);
-                if (lane >= static_cast<uint32_t>(d)) {
-                    wa += na;
-                    wb += nb;
-                }
-            }
-            s_a[lane] = wa;
-            s_b[lane] = wb;
-        }
-        __syncthreads();
-        uint32_t ra = carryA + ia - a + (warp ? s_a[warp - 1] : 0u);
-        uint32_t rb = carryB + ib - b + (warp ? s_b[warp - 1] : 0u);
-#pragma unroll
-        for (uint32_t j = 0; j < kPer; ++j) {
-            if (t0 + j < p.tiles) p.tilePrefix[t0 + j] = make_uint2(ra, rb);
-            ra += v[j].x;
-            rb += v[j].y;
-        }
-        carryA += s_a[31];
-        carryB += s_b[31];
-        __syncthreads();  // s_a, s_b are reused
-    }
+// ORs a 32-slot ballot whose first slot is s0 into the slot-ordered visibility words (the ballot
+// straddles two words unless s0 is a multiple of 32).
+__device__ __forceinline__ void or_bits(uint32_t* bits, uint32_t s0, uint32_t bal) {
+    if (bal == 0u) return;
+    const uint32_t sh = s0 & 31u;
+    atomicOr(bits + (s0 >> 5), bal << sh);
+    if (sh != 0u && (bal >> (32u - sh)) != 0u) atomicOr(bits + (s0 >> 5) + 1u, bal >> (32u - sh));
 }
 
-// Test launch: `split` blocks per tile, block `part` taking the tile's 256-slot chunks part,
-// part + split, ... so that a tile with many candidates spreads over several SMs. Each chunk
-// stores its eight visibility words and survivors are added to the tile's count (task form: to
-// the objects' counts, each visibility word split at the object boundaries inside it).
+// Test launch, a persistent grid of warps over the work list, one item per warp at a time: lane l
+// tests the item's clusters l and l + 32 (two independent chains of loads and arithmetic), all of
+// one object, whose transform every lane reads from the same address. The object and the cluster
+// table rows are contiguous, so the loads coalesce and no lane searches for its object. Visible
+// clusters set their bits (slot order) and count towards their tile (task form: towards their
+// object, and the tile's tasks and payloads grow by what the object's new count adds: a task when
+// it leaves zero, a payload per 32 survivors; the additions telescope to the final counts whatever
+// the order of the items), and towards the frame's totals.
 template <bool TASKS>
 __global__ void __launch_bounds__(kClThreads) cluster_test_kernel(const ClusterParams p, const BlzCameraViewData view) {
-    static_assert(kClObjects == 32, "the tile's objects are one warp");
-    __shared__ float4 s_xf[kClObjects][2];
-    __shared__ uint32_t s_off[kClObjects];
-    __shared__ uint32_t s_start[kClObjects + 1];
-    __shared__ uint32_t s_warp[kClWarps];
-    __shared__ uint32_t s_surv[kClObjects];
-    const uint32_t tile = blockIdx.x / p.split, part = blockIdx.x - tile * p.split;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t T = __ldcg(p.tileSlots + tile);
-    if (part * static_cast<uint32_t>(kClThreads) >= T) return;  // no chunk for this block
-    if (warp == 0) {
-        const uint32_t o = tile * kClObjects + lane;
-        const uint2 info = __ldcg(p.objInfo + o);
-        s_xf[lane][0] = __ldcg(p.objXf + 2u * o);
-        s_xf[lane][1] = __ldcg(p.objXf + 2u * o + 1u);
-        uint32_t incl = info.y;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-            if (lane >= static_cast<uint32_t>(d)) incl += n;
-        }
-        s_start[lane] = incl - info.y;
-        if (lane == 31) s_start[kClObjects] = incl;
-        s_off[lane] = info.x;
-        s_surv[lane] = 0u;
-    }
-    __syncthreads();
+    const uint32_t nItems = __ldcg(p.itemCount);
     const ViewConsts v = load_view(view);
-    uint32_t* bits = p.bits + static_cast<size_t>(tile) * p.bitWords;
-    uint32_t survivors = 0;
-    for (uint32_t chunk = part * kClThreads; chunk < T; chunk += p.split * kClThreads) {
-        const uint32_t slot = chunk + threadIdx.x;
-        bool vis = false;
-        uint32_t lo = 0;
-        if (slot < T) {
-            lo = slot_object(s_start, slot);
-            vis = cluster_visible(p, v, s_xf[lo][0], s_xf[lo][1], s_off[lo] + (slot - s_start[lo]));
-        }
-        uint32_t bal = __ballot_sync(0xFFFFFFFFu, vis);
-        if (lane == 0 && bal != 0u) {
-            bits[(chunk >> 5) + warp] = bal;
+    const uint32_t warpsTotal = gridDim.x * kClWarps;
+    for (uint32_t it = blockIdx.x * kClWarps + warp; it < nItems; it += warpsTotal) {
+        const uint4 item = __ldcg(p.items + it);  // {object, first cluster, first slot, clusters}
+        const uint32_t o = item.x;
+        const float4 ps = __ldcg(p.objXf + 2u * o), q = __ldcg(p.objXf + 2u * o + 1u);
+        bool v0 = false, v1 = false;
+        if (lane < item.w) v0 = cluster_visible(p, v, ps, q, item.y + lane);
+        if (lane + 32u < item.w) v1 = cluster_visible(p, v, ps, q, item.y + 32u + lane);
+        const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, v0), b1 = __ballot_sync(0xFFFFFFFFu, v1);
+        const uint32_t add = static_cast<uint32_t>(__popc(b0) + __popc(b1));
+        if (add != 0u && lane == 0) {
+            const uint32_t tile = o / kClObjects;
+            uint32_t* bits = p.bits + static_cast<size_t>(tile) * p.bitWords;
+            or_bits(bits, item.z, b0);
+            or_bits(bits, item.z + 32u, b1);
             if constexpr (TASKS) {
-                // the word's set bits per object, from lane 0's object on
-                const uint32_t slot0 = chunk + 32u * warp;
-                while (bal != 0u && lo < kClObjects) {
-                    const uint32_t n = min(32u, s_start[lo + 1u] - slot0);  // low bits in objects <= lo
-                    const uint32_t mask = n >= 32u ? 0xFFFFFFFFu : (1u << n) - 1u;
-                    const uint32_t c = __popc(bal & mask);
-                    if (c != 0u) atomicAdd(&s_surv[lo], c);
-                    bal &= ~mask;
-                    ++lo;
+                const uint32_t old = atomicAdd(p.objSurv + o, add);
+                if (old == 0u) {
+                    atomicAdd(p.tileCount + 2u * tile, 1u);
+                    atomicAdd(&p.totals->x, 1u);
+                }
+                const uint32_t dp = (old + add + 31u) / 32u - (old + 31u) / 32u;
+                if (dp != 0u) {
+                    atomicAdd(p.tileCount + 2u * tile + 1u, dp);
+                    atomicAdd(&p.totals->y, dp);
                 }
             } else {
-                survivors += __popc(bal);
+                atomicAdd(p.tileCount + 2u * tile, add);
+                atomicAdd(&p.totals->x, add);
             }
-        } else if (lane == 0 && chunk + 32u * warp < T) {
-            bits[(chunk >> 5) + warp] = 0u;
         }
     }
-    if constexpr (!TASKS) {
-        if (lane == 0) s_warp[warp] = survivors;
-    }
-    __syncthreads();
-    if constexpr (TASKS) {
-        if (warp == 0 && s_surv[lane] != 0u) atomicAdd(p.objSurv + tile * kClObjects + lane, s_surv[lane]);
-    } else if (threadIdx.x == 0) {
-        uint32_t total = 0;
-        for (int w = 0; w < kClWarps; ++w) total += s_warp[w];
-        if (total != 0u) atomicAdd(p.tileCount + 2u * tile, total);
-    }
 }
 
-// Task form, one warp per tile: the tile's {tasks, payloads} from its objects' survivor counts.
-__global__ void __launch_bounds__(kClThreads) cluster_task_totals_kernel(const ClusterParams p) {
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t tile = blockIdx.x * kClWarps + warp;
-    if (tile >= p.tiles) return;
-    const uint32_t sv = __ldcg(p.objSurv + tile * kClObjects + lane);
-    const uint32_t tasks = __popc(__ballot_sync(0xFFFFFFFFu, sv != 0u));
-    const uint32_t payloads = __reduce_add_sync(0xFFFFFFFFu, (sv + 31u) >> 5);
-    if (lane == 0) reinterpret_cast<uint2*>(p.tileCount)[tile] = make_uint2(tasks, payloads);
-}
-
-// Emit launch, one warp per tile (lane = object): no test is repeated. The tile's cluster ranges,
-// visibility bits and the records (task form: tasks and payloads) before it come from the earlier
-// launches; every set bit is written at its final position in slot order, the tile's set bits
-// spread over the lanes 32 at a time.
+// Emit launch, one warp per tile (lane = object): no test is repeated. The last tile's warp writes
+// the frame's counts; a tile without records returns. The tile's cluster ranges, visibility bits
+// and counts come from the earlier launches, the records (task form: tasks and payloads) before it
+// from the counts of the tiles before it; every set bit is written at its final position in slot
+// order, the tile's set bits spread over the lanes 32 at a time.
 template <bool TASKS>
 __global__ void __launch_bounds__(kClThreads) cluster_emit_kernel(const ClusterParams p) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -318,12 +236,47 @@ __global__ void __launch_bounds__(kClThreads) cluster_emit_kernel(const ClusterP
     const uint32_t lt = lanemask_lt();
     const uint32_t* bits = p.bits + static_cast<size_t>(tile) * p.bitWords;
 
+    // the frame's totals (counted by the test launch) and, from the last tile, the rewind of the
+    // work list, which the test launch has finished reading
+    if (tile == p.tiles - 1u && lane == 0) {
+        const uint2 tot = __ldcg(p.totals);
+        if constexpr (TASKS) {
+            *p.taskCount = tot.x;
+            *p.payloadCount = tot.y;
+            if (tot.x > p.taskCapacity || tot.y > p.payloadCapacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
+        } else {
+            *p.drawCount = tot.x;
+            if (tot.x > p.capacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
+        }
+        *p.itemCount = 0u;
+    }
+    // a tile without records (task form: without tasks, so without payloads) writes nothing
+    const uint2* tc = reinterpret_cast<const uint2*>(p.tileCount);
+    if (__ldcg(tc + tile).x == 0u) return;
+
     // independent loads first
     const uint32_t T = __ldcg(p.tileSlots + tile);
     const uint32_t bFirst = lane < p.bitWords ? __ldcg(bits + lane) : 0u;
     const uint2 info = __ldcg(p.objInfo + tile * kClObjects + lane);  // {clusterOffset, count}
-    const uint2 pre = __ldcg(p.tilePrefix + tile);                    // records (tasks, payloads) before the tile
     const uint32_t sv = TASKS ? __ldcg(p.objSurv + tile * kClObjects + lane) : 0u;
+    // records (task form: tasks, payloads) before the tile: the counts of the tiles before it,
+    // summed by the warp, kClPrefixLoads loads per lane in flight
+    uint2 pre = make_uint2(0u, 0u);
+    for (uint32_t t0 = 0; t0 < tile; t0 += 32u * kClPrefixLoads) {
+        uint2 x[kClPrefixLoads];
+#pragma unroll
+        for (uint32_t j = 0; j < kClPrefixLoads; ++j) {
+            const uint32_t t = t0 + j * 32u + lane;
+            x[j] = t < tile ? __ldcg(tc + t) : make_uint2(0u, 0u);
+        }
+#pragma unroll
+        for (uint32_t j = 0; j < kClPrefixLoads; ++j) {
+            pre.x += x[j].x;
+            pre.y += x[j].y;
+        }
+    }
+    pre.x = __reduce_add_sync(0xFFFFFFFFu, pre.x);
+    pre.y = __reduce_add_sync(0xFFFFFFFFu, pre.y);
 
     uint32_t incl = info.y;
 #pragma unroll
@@ -363,12 +316,6 @@ __global__ void __launch_bounds__(kClThreads) cluster_emit_kernel(const ClusterP
                 uint32_t* pw = p.payloads + static_cast<size_t>(last) * 33u + 1u;
                 for (uint32_t e = tail; e < 32u; ++e) pw[e] = BLZ_NO_MESHLET;
             }
-        }
-        if (lane == 31 && tile == p.tiles - 1u) {
-            const uint32_t nt = pre.x + __popc(has), np = pre.y + ik;
-            *p.taskCount = nt;
-            *p.payloadCount = np;
-            if (nt > p.taskCapacity || np > p.payloadCapacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
         }
     }
 
@@ -425,12 +372,6 @@ __global__ void __launch_bounds__(kClThreads) cluster_emit_kernel(const ClusterP
         }
         run += roundTotal;
     }
-    if constexpr (!TASKS) {
-        if (lane == 0 && tile == p.tiles - 1u) {
-            *p.drawCount = run;
-            if (run > p.capacity) atomicOr(&p.scratch->status, BLZ_FLAG_COMMAND_OVERFLOW);
-        }
-    }
 }
 
 uint32_t cluster_tile_objects() { return kClObjects; }
@@ -440,26 +381,26 @@ static cudaError_t launch_cluster(const ClusterParams& p, const BlzCameraViewDat
     cluster_object_kernel<TASKS><<<(p.tiles + kClWarps - 1) / kClWarps, kClThreads, 0, s>>>(p, view);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    cluster_test_kernel<TASKS><<<p.tiles * p.split, kClThreads, 0, s>>>(p, view);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    if constexpr (TASKS) {
-        cluster_task_totals_kernel<<<(p.tiles + kClWarps - 1) / kClWarps, kClThreads, 0, s>>>(p);
-        e = cudaGetLastError();
+    // the test launch: every resident warp at once, or one warp per item when there are fewer
+    static int perSm = 0;
+    if (perSm == 0) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, cluster_test_kernel<TASKS>, kClThreads, 0);
         if (e != cudaSuccess) return e;
+        if (perSm < 1) perSm = 1;
     }
-    cluster_scan_kernel<<<1, kScanThreads, 0, s>>>(p);
+    const uint64_t maxItems = cluster_max_items(p.tiles, p.bitWords);
+    uint64_t blocks = static_cast<uint64_t>(perSm) * (p.smCount > 0 ? p.smCount : 1);
+    blocks = std::min<uint64_t>(blocks, (maxItems + kClWarps - 1) / kClWarps);
+    cluster_test_kernel<TASKS><<<static_cast<uint32_t>(blocks ? blocks : 1), kClThreads, 0, s>>>(p, view);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     cluster_emit_kernel<TASKS><<<(p.tiles + kClWarps - 1) / kClWarps, kClThreads, 0, s>>>(p);
     return cudaGetLastError();
 }
 
-uint32_t cluster_split(uint32_t lodClusterMax) {
-    // blocks per tile: enough that the most a tile can hold (32 objects x the largest LOD) spreads
-    // over several SMs, at most kClMaxSplit
-    const uint32_t chunks = (kClObjects * lodClusterMax + kClThreads - 1) / kClThreads;
-    return chunks < 1u ? 1u : (chunks > kClMaxSplit ? kClMaxSplit : chunks);
+uint64_t cluster_max_items(uint32_t tiles, uint32_t lodClusterMax) {
+    // every object of every tile with the longest cluster range, in items of kClItem clusters
+    return static_cast<uint64_t>(tiles) * kClObjects * ((std::max<uint32_t>(lodClusterMax, 1u) + kClItem - 1) / kClItem);
 }
 
 cudaError_t launch_cluster_cull(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s) {

@@ -169,6 +169,9 @@ struct ClusterParams {
     uint32_t* drawCount;
     Scratch* scratch;
     uint32_t* tileCount;  // scratch [tiles] uint2: {surviving clusters, 0} per tile (task form: {tasks, payloads})
+    uint4* items;         // scratch: the test launch's work list, {object, first cluster, first slot, clusters}
+    uint32_t* itemCount;  // scratch, one word: items in the list (zero between launches)
+    uint2* totals;        // scratch: the frame's records (task form: {tasks, payloads}), counted by the test launch
     // task form (blz_cull_cluster_tasks)
     uint32_t* tasks;         // BlzIndirectTask words, 4 per task
     uint32_t* payloads;      // BlzMeshTaskPayload words, 33 per payload
@@ -182,9 +185,8 @@ struct ClusterParams {
     uint32_t* bits;          // scratch [tiles * bitWords]: one visibility bit per candidate cluster, slot order
     uint32_t bitWords;       // words per tile: >= 32 objects x the largest LOD cluster count / 32
     uint32_t tiles;          // tiles of 32 objects
-    uint32_t split;          // test blocks per tile
+    uint32_t smCount;        // the device's SMs (the test launch is one wave of resident blocks)
     uint32_t* tileSlots;     // scratch [tiles]: candidate clusters of the tile
-    uint2* tilePrefix;       // scratch [tiles]: records (task form: {tasks, payloads}) before the tile
 };
 
 struct PyramidBuildParams {
@@ -248,7 +250,8 @@ cudaError_t launch_instanced_staged(const PipeParams& p, const InstStagedParams&
                                     int smCount, cudaStream_t s);
 cudaError_t launch_instanced_cull(const InstancedParams& p, const BlzCameraViewData& view, cudaStream_t s);
 uint32_t cluster_tile_objects();
-uint32_t cluster_split(uint32_t lodClusterMax);
+// Upper bound of the cluster test launch's work items for `tiles` tiles.
+uint64_t cluster_max_items(uint32_t tiles, uint32_t lodClusterMax);
 cudaError_t launch_cluster_cull(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s);
 cudaError_t launch_cluster_tasks(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s);
 cudaError_t launch_pyramid_build(const PyramidBuildParams& p, cudaStream_t s, uint32_t* launches);

@@ -155,6 +155,26 @@ def test_clusters_match_oracle(cluster_ctx, with_hiz):
     assert np.array_equal(ids[:n].cpu().numpy().view(np.uint32), oids)
 
 
+def test_clusters_repeated_calls_of_changing_size(cluster_ctx):
+    """The test launch's finished-block counts (per tile and over the tiles) are rewound by the
+    blocks that finish them: calls of different list sizes in a row, with and without Hi-Z, each
+    match the oracle."""
+    c, sc = cluster_ctx
+    v = view_for(zfar=1e4, position=(0.0, 0.0, -50.0))
+    pyr, opyr = _cluster_pyramid(c, sc, v)
+    rng = np.random.default_rng(8)
+    for k, size in enumerate([sc.count, 33, 5_000, 1, sc.count, 2_017]):
+        objs = sc.objects if size == sc.count else sc.objects[rng.permutation(sc.count)[:size]]
+        dobjs = to_device(objs, "cuda")
+        with_hiz = k % 2 == 1
+        cap = max(O._cluster_upper_bound(sc, objs), 1)
+        t = Target.alloc(cap)
+        c.cluster_cull(v, t, pyramid=pyr if with_hiz else None, objects=dobjs, count=len(objs))
+        assert c.check() == 0
+        n, recs, _, _ = O.cull_clusters(v, sc, pyramid=opyr if with_hiz else None, capacity=cap, objects=objs)
+        assert_records_equal(t.read(), (n, recs), f"call {k} ({size} objects)")
+
+
 def test_cluster_cone_test_culls_something(cluster_ctx):
     c, sc = cluster_ctx
     v = view_for(zfar=1e4, position=(0.0, 0.0, -50.0))
