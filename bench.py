@@ -537,6 +537,23 @@ def main():
 
     t_e2e_sep, _ = zero_copy_run(step_graphs["separate_calls"])
     t_e2e, counts = zero_copy_run(step_graphs["kept_frame"])
+
+    # the CPU-GPU link's host-to-device rate, measured here: the step's depth upload alone (pinned
+    # host buffer, one copy-engine copy), median of 20; the e2e step cannot finish before this upload
+    # and the work that needs the depth (pyramid, pass 2) are done
+    link_ms = []
+    for _ in range(23):
+        torch.cuda.synchronize()
+        e0.record()
+        depth.copy_(hdepth, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        link_ms.append(e0.elapsed_time(e1))
+    link_ms = statistics.median(link_ms[3:])
+    link = {"h2d_GBs": W * H * 4 / (link_ms * 1e-3) / 1e9, "depth_upload_ms": link_ms,
+            "upload_share_of_step": link_ms / t_e2e,
+            "note": "measured host-to-device rate of the CPU-GPU link (8.3 MB depth copy from pinned memory); "
+                    "the step's critical path is the upload, then the pyramid and pass 2 (pass 1 runs beside it)"}
     # the last recorded step against the oracle on the scene as that step saw it (its dynamic rows)
     edited = S.Scene(sc.objects, sc.transforms.copy(), sc.surfaces, sc.lods, visibility=sc.visibility)
     edited.transforms[:DYNAMIC] = h_tr_np
@@ -555,6 +572,7 @@ def main():
                    "(blz_scene_bind_dynamic); one blz_graph_launch of the recorded step: depth upload + pyramid beside "
                    "blz_frame_first, then blz_frame_late; both passes read the rows over the CPU-GPU link; draw "
                    "counts written to pinned memory",
+           "link": link,
            "separate_calls": {"value": job_throughput(N, world, t_e2e_sep), "ms_per_step": t_e2e_sep,
                               "path": "the same step with blz_cull_first / blz_cull_late"},
            "with_copies": {"value": job_throughput(N, world, t_e2e_copies), "ms_per_step": t_e2e_copies,
