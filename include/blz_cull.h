@@ -143,8 +143,8 @@ typedef struct BlzSceneDesc {
  * Borrowed device tables must be aligned: transforms to 32 bytes (one transform is read in a
  * single 32-byte load), surfaces, LODs and clusters to 16, render objects to 8.
  * The LOD table is read once here (a borrowed one too, synchronously) for its largest cluster
- * range, which sizes the cluster cull's visibility bits: a LOD whose clusterCount is raised past
- * that afterwards makes the cluster culls skip the objects around it and raise
+ * range, which sizes the cluster cull's visibility bits and work list: an object whose chosen LOD's
+ * clusterCount was raised past that afterwards emits nothing from the cluster culls, which raise
  * BLZ_FLAG_BAD_INDEX. */
 int blz_scene_upload(blz_ctx* ctx, const BlzSceneDesc* scene, uint32_t flags, blz_stream_t stream);
 
