@@ -525,6 +525,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) cull_frame_kernel(con
 // rewinds the decide kernel's work counter for the next launch.
 constexpr int kScatterWarps = 32;  // one warp per chunk
 constexpr uint32_t kScatterChunks = 32;
+constexpr uint32_t kScatterPre = 2;  // 32-record slices of its chunk a warp loads before the offsets are known
 
 template <bool SINGLE>
 __device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_t block) {
@@ -537,26 +538,35 @@ __device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_
     if (c0 >= p.totalTiles) return;
     const uint32_t vi0 = SINGLE ? 0u : find_view_warp(p.tileStart, p.viewCount, c0);
     const uint32_t viewStart0 = SINGLE ? 0u : __ldg(p.tileStart + vi0);
-    // 0. each warp fetches its chunk's first 2 * 32 staged records and their LODs now, so those
-    //    loads overlap the offset computation below
+    // 0. each warp fetches its chunk's first kScatterPre * 32 staged records and their LODs now, so
+    //    those loads overlap the offset computation below
     const uint32_t myChunk = c0 + warp;
     const uint32_t myN = myChunk < p.totalTiles ? __ldcg(p.chunkCount + myChunk) : 0u;
     const uint2* myStage = p.staged + static_cast<size_t>(myChunk) * chunkSize;
-    uint2 pre[2], preLod[2];
+    uint2 pre[kScatterPre], preLod[kScatterPre];
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
+    for (uint32_t u = 0; u < kScatterPre; ++u) {
         const uint32_t i = lane + 32u * u;
         pre[u] = i < myN ? __ldcg(myStage + i) : make_uint2(0u, 0u);
     }
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
+    for (uint32_t u = 0; u < kScatterPre; ++u) {
         const uint32_t i = lane + 32u * u;
         preLod[u] = i < myN ? __ldg(reinterpret_cast<const uint2*>(p.sc.lods + pre[u].y)) : make_uint2(0u, 0u);
     }
     // 1. records of the first chunk's view before c0; each warp also hands its chunk's count to
     //    warp 0 through shared memory
     uint32_t part = 0;
-    for (uint32_t c = viewStart0 + threadIdx.x; c < c0; c += kScatterWarps * 32) part += __ldcg(p.chunkCount + c);
+    for (uint32_t c = viewStart0 + threadIdx.x; c < c0; c += 8u * kScatterWarps * 32u) {
+        uint32_t x[8];  // eight loads in flight per thread
+#pragma unroll
+        for (uint32_t k = 0; k < 8u; ++k) {
+            const uint32_t ck = c + k * kScatterWarps * 32u;
+            x[k] = ck < c0 ? __ldcg(p.chunkCount + ck) : 0u;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < 8u; ++k) part += x[k];
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
     if (lane == 0) {
@@ -621,12 +631,12 @@ __device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_
     // staged record i goes to slot base + i, or base + n - 1 - i for a chunk staged last object first
     const bool down = SINGLE && p.descending != 0u;
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
+    for (uint32_t u = 0; u < kScatterPre; ++u) {
         const uint32_t i = lane + 32u * u;
         const uint32_t slot = base + (down ? myN - 1u - i : i);
         if (i < myN && slot < bv.capacity) put_record(bv.cmds, bv.stride, slot, pre[u].x, preLod[u].x, preLod[u].y);
     }
-    for (uint32_t i = lane + 64u; i < myN; i += 32) {
+    for (uint32_t i = lane + 32u * kScatterPre; i < myN; i += 32) {
         const uint32_t slot = base + (down ? myN - 1u - i : i);
         if (slot >= bv.capacity) {
             if (down) continue;
