@@ -95,6 +95,20 @@ __device__ __forceinline__ void wait_pyramid(const unsigned int* ready, uint32_t
     __syncwarp();
 }
 
+// The lanes of the warp whose record has the same LOD id as this lane's (ids below 2^bits): one
+// ballot per bit of the id, each lane keeping the lanes that agree with it on every bit. Votes, not
+// a match instruction, so the ranking stays off the shared-memory pipe. Lanes without a record
+// (valid false) get a mask their callers do not use.
+__device__ __forceinline__ unsigned same_lod_lanes(uint32_t b, uint32_t bits, bool valid) {
+    unsigned m = __ballot_sync(0xFFFFFFFFu, valid);
+    for (uint32_t k = 0; k < bits; ++k) {
+        const bool bit = ((b >> k) & 1u) != 0u;
+        const unsigned v = __ballot_sync(0xFFFFFFFFu, bit);
+        m &= bit ? v : ~v;
+    }
+    return m;
+}
+
 // Dense stage over one survivor per lane (lanes with `mine`), in object order: the sphere
 // projection and Hi-Z test (LATE/TEMPORAL), LATE's visibility write, LOD selection of the emitted
 // ones, and their staging as (objectId, lodId) after the `run` already staged for the chunk.
@@ -142,7 +156,8 @@ __device__ __forceinline__ void dense_entry(const SceneTables& sc, const BatchVi
     run += __popc(e);
     if constexpr (MODE == kModeInstanced) {
         // the group's histogram row (hist = row of this chunk's group): one add per distinct LOD
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, emitted ? lid : 0xFFFFFFFFu);
+        const uint32_t idBits = sc.lodCount > 1u ? 32u - static_cast<uint32_t>(__clz(static_cast<int>(sc.lodCount - 1u))) : 0u;
+        const unsigned peers = same_lod_lanes(lid, idBits, emitted);
         if (emitted && (peers & lanemask_lt()) == 0u) atomicAdd(hist + lid, static_cast<uint32_t>(__popc(peers)));
     }
     if constexpr (FUSED) {
@@ -964,11 +979,12 @@ cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t thre
 //            which has no group before it, sums all of them instead, which gives every LOD's total,
 //            and writes the counters and, in ascending LOD order, one command per non-empty LOD;
 //   rows     each warp counts its chunk's records per LOD, and the block scans those rows per LOD;
-//   place    each warp places its records in order (ranks inside 32-record slices from
-//            __match_any_sync).
+//   place    each warp places its records in order (ranks inside 32-record slices from one
+//            ballot per bit of the LOD id).
 
 constexpr uint32_t kInstBatch = 4;  // 32-record slices whose loads are issued together
 constexpr uint32_t kInstThreads = kInstGroup * 32;
+
 
 __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStagedParams q) {
     // [kInstGroup][nL] per-warp counts, then offsets; [nL] the group's offset in each LOD's list;
@@ -997,10 +1013,13 @@ __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStag
     };
     uint2 first[kInstBatch];  // the chunk's first 128 records, loaded once for both walks
     load_batch(0, first);
+    // LOD threadIdx.x's instanceOffset (nL <= kInstThreads), stored to shared memory once phase 1
+    // is done, so no barrier waits for the load
+    const uint32_t ioff = threadIdx.x < nL ? __ldg(&q.counters[threadIdx.x].instanceOffset) : 0u;
+    const uint32_t idBits = nL > 1u ? 32u - static_cast<uint32_t>(__clz(static_cast<int>(nL - 1u))) : 0u;
     for (uint32_t b = threadIdx.x; b < nL; b += kInstThreads) {
         s_goff[b] = 0u;
         s_tot[b] = 0u;
-        s_ioff[b] = __ldg(&q.counters[b].instanceOffset);
     }
     for (uint32_t j = threadIdx.x; j < kInstGroup * nL; j += kInstThreads) s_rows[j] = 0u;
     if (threadIdx.x == 0) s_flags = 0u;
@@ -1035,11 +1054,12 @@ __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStag
 #pragma unroll
         for (uint32_t k = 0; k < kInstBatch; ++k) {
             const uint32_t b = r[k].y;
-            const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
+            const unsigned peers = same_lod_lanes(b, idBits, b != 0xFFFFFFFFu);
             if (b != 0xFFFFFFFFu && (peers & lt) == 0u) row[b] += __popc(peers);
             __syncwarp();
         }
     }
+    if (threadIdx.x < nL) s_ioff[threadIdx.x] = ioff;
     __syncthreads();
     // 2. per LOD, exclusive offsets of the warps' chunks inside the group: row tr of threads sums
     //    its kInstGroup / R consecutive warps' counts, then scans them after the sums of the rows
@@ -1076,7 +1096,7 @@ __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStag
 #pragma unroll
         for (uint32_t k = 0; k < kInstBatch; ++k) {
             const uint32_t b = r[k].y;
-            const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
+            const unsigned peers = same_lod_lanes(b, idBits, b != 0xFFFFFFFFu);
             uint32_t before = 0;
             if (b != 0xFFFFFFFFu) before = row[b];
             __syncwarp();
