@@ -251,7 +251,9 @@ def serving(culler, scene, device, seconds=2.0, rates=(2000.0, 8000.0, 20000.0, 
 
 
 def _replay_ms(culler, fn, reps, flush, stream) -> float:
-    """Median CUDA-event time of `fn` recorded once and replayed as a graph, L2 flushed before each."""
+    """Mean CUDA-event time of `fn` recorded once and replayed as a graph, L2 flushed before each.
+    The mean, not the median: the event timer advances in steps of about 2 us on these GPUs, so a
+    median snaps to one of those steps while the mean of many replays resolves finer."""
     with torch.cuda.stream(stream):
         fn()
         culler.capture_begin()
@@ -269,7 +271,7 @@ def _replay_ms(culler, fn, reps, flush, stream) -> float:
             b.synchronize()
             times.append(a.elapsed_time(b))
         g.close()
-    return float(np.median(times))
+    return float(np.mean(times))
 
 
 def instanced(culler, scene, device, reps=30, slots=100_000) -> dict:

@@ -121,13 +121,14 @@ int bind_cluster_scratch(blz_ctx* c, uint32_t tiles, ClusterParams& p) {
     auto r256 = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t headBytes = 256;
     const size_t countBytes = r256(static_cast<size_t>(tiles) * sizeof(uint2));
+    const size_t superBytes = r256(static_cast<size_t>(cluster_tile_groups(tiles)) * sizeof(uint2));
     const size_t tileBytes = r256(static_cast<size_t>(tiles) * sizeof(uint32_t));
     const size_t infoBytes = r256(objs * sizeof(uint2));
     const size_t xfBytes = r256(objs * 2 * sizeof(float4));
     const size_t survBytes = r256(objs * sizeof(uint32_t));
     const size_t itemBytes = r256(static_cast<size_t>(cluster_max_items(tiles, bitWords)) * sizeof(uint4));
     const size_t bitBytes = static_cast<size_t>(tiles) * bitWords * sizeof(uint32_t);
-    const size_t need = headBytes + countBytes + tileBytes + infoBytes + xfBytes + survBytes + itemBytes + bitBytes;
+    const size_t need = headBytes + countBytes + superBytes + tileBytes + infoBytes + xfBytes + survBytes + itemBytes + bitBytes;
     if (need > c->clusterBytes) {
         if (c->capturing) return fail(BLZ_ERR_CAPACITY, "scratch must grow, which a capture cannot record: run the call once before capturing");
         if (c->clusterMem) {
@@ -153,6 +154,8 @@ int bind_cluster_scratch(blz_ctx* c, uint32_t tiles, ClusterParams& p) {
     m += headBytes;
     p.tileCount = reinterpret_cast<uint32_t*>(m);
     m += countBytes;
+    p.superCount = reinterpret_cast<uint2*>(m);
+    m += superBytes;
     p.tileSlots = reinterpret_cast<uint32_t*>(m);
     m += tileBytes;
     p.objInfo = reinterpret_cast<uint2*>(m);

@@ -32,7 +32,8 @@ constexpr int kClThreads = 256;
 constexpr int kClWarps = kClThreads / 32;
 constexpr uint32_t kClObjects = 32;  // objects per tile
 constexpr uint32_t kClItem = 64;     // clusters per work item of the test launch (two per lane)
-constexpr uint32_t kClPrefixLoads = 16;  // emit launch: tile counts each lane loads at once
+constexpr uint32_t kClSuper = 64;     // tiles per group whose counts the test launch also sums
+constexpr uint32_t kClPrefixLoads = 4;   // emit launch: group and tile counts each lane loads at once
 
 // Sphere, Hi-Z and cone tests of one cluster of an object. The int8 cone axis and cutoff are divided
 // by 127 only for the clusters that reach the cone test (about 2 % of them behind the occluders of a
@@ -160,6 +161,7 @@ __global__ void __launch_bounds__(kClThreads) cluster_object_kernel(const Cluste
     p.objXf[2u * i + 1u] = quat;
     flags = __reduce_or_sync(0xFFFFFFFFu, flags);
     if (tile == 0u && lane == 0) *p.totals = make_uint2(0u, 0u);
+    if (tile % kClSuper == 0u && lane == 0) p.superCount[tile / kClSuper] = make_uint2(0u, 0u);
     if (lane == 0) {
         p.tileSlots[tile] = total;
         reinterpret_cast<uint2*>(p.tileCount)[tile] = make_uint2(0u, 0u);
@@ -208,15 +210,18 @@ __global__ void __launch_bounds__(kClThreads) cluster_test_kernel(const ClusterP
                 const uint32_t old = atomicAdd(p.objSurv + o, add);
                 if (old == 0u) {
                     atomicAdd(p.tileCount + 2u * tile, 1u);
+                    atomicAdd(&p.superCount[tile / kClSuper].x, 1u);
                     atomicAdd(&p.totals->x, 1u);
                 }
                 const uint32_t dp = (old + add + 31u) / 32u - (old + 31u) / 32u;
                 if (dp != 0u) {
                     atomicAdd(p.tileCount + 2u * tile + 1u, dp);
+                    atomicAdd(&p.superCount[tile / kClSuper].y, dp);
                     atomicAdd(&p.totals->y, dp);
                 }
             } else {
                 atomicAdd(p.tileCount + 2u * tile, add);
+                atomicAdd(&p.superCount[tile / kClSuper].x, add);
                 atomicAdd(&p.totals->x, add);
             }
         }
@@ -259,20 +264,27 @@ __global__ void __launch_bounds__(kClThreads) cluster_emit_kernel(const ClusterP
     const uint32_t bFirst = lane < p.bitWords ? __ldcg(bits + lane) : 0u;
     const uint2 info = __ldcg(p.objInfo + tile * kClObjects + lane);  // {clusterOffset, count}
     const uint32_t sv = TASKS ? __ldcg(p.objSurv + tile * kClObjects + lane) : 0u;
-    // records (task form: tasks, payloads) before the tile: the counts of the tiles before it,
-    // summed by the warp, kClPrefixLoads loads per lane in flight
+    // records (task form: tasks, payloads) before the tile: the counts of the groups of kClSuper
+    // tiles before its group, then of the tiles of its group before it, all loaded at once
     uint2 pre = make_uint2(0u, 0u);
-    for (uint32_t t0 = 0; t0 < tile; t0 += 32u * kClPrefixLoads) {
+    {
+        const uint32_t sg = tile / kClSuper, t0 = sg * kClSuper;
         uint2 x[kClPrefixLoads];
 #pragma unroll
         for (uint32_t j = 0; j < kClPrefixLoads; ++j) {
-            const uint32_t t = t0 + j * 32u + lane;
-            x[j] = t < tile ? __ldcg(tc + t) : make_uint2(0u, 0u);
+            const uint32_t i = j * 32u + lane;  // i < sg: group i; then tile t0 + (i - sg) while below `tile`
+            if (i < sg) x[j] = __ldcg(p.superCount + i);
+            else x[j] = t0 + (i - sg) < tile ? __ldcg(tc + t0 + (i - sg)) : make_uint2(0u, 0u);
         }
 #pragma unroll
         for (uint32_t j = 0; j < kClPrefixLoads; ++j) {
             pre.x += x[j].x;
             pre.y += x[j].y;
+        }
+        for (uint32_t i = kClPrefixLoads * 32u + lane; i < sg + (tile - t0); i += 32u) {  // more groups than one round holds
+            const uint2 y = i < sg ? __ldcg(p.superCount + i) : __ldcg(tc + t0 + (i - sg));
+            pre.x += y.x;
+            pre.y += y.y;
         }
     }
     pre.x = __reduce_add_sync(0xFFFFFFFFu, pre.x);
@@ -375,6 +387,8 @@ __global__ void __launch_bounds__(kClThreads) cluster_emit_kernel(const ClusterP
 }
 
 uint32_t cluster_tile_objects() { return kClObjects; }
+
+uint32_t cluster_tile_groups(uint32_t tiles) { return (tiles + kClSuper - 1) / kClSuper; }
 
 template <bool TASKS>
 static cudaError_t launch_cluster(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s) {

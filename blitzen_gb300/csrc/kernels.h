@@ -172,6 +172,7 @@ struct ClusterParams {
     uint4* items;         // scratch: the test launch's work list, {object, first cluster, first slot, clusters}
     uint32_t* itemCount;  // scratch, one word: items in the list (zero between launches)
     uint2* totals;        // scratch: the frame's records (task form: {tasks, payloads}), counted by the test launch
+    uint2* superCount;    // scratch [cluster_tile_groups(tiles)]: the same counts per group of tiles
     // task form (blz_cull_cluster_tasks)
     uint32_t* tasks;         // BlzIndirectTask words, 4 per task
     uint32_t* payloads;      // BlzMeshTaskPayload words, 33 per payload
@@ -250,6 +251,8 @@ cudaError_t launch_instanced_staged(const PipeParams& p, const InstStagedParams&
                                     int smCount, cudaStream_t s);
 cudaError_t launch_instanced_cull(const InstancedParams& p, const BlzCameraViewData& view, cudaStream_t s);
 uint32_t cluster_tile_objects();
+// Groups of tiles whose counts the cluster test launch also sums, for `tiles` tiles.
+uint32_t cluster_tile_groups(uint32_t tiles);
 // Upper bound of the cluster test launch's work items for `tiles` tiles.
 uint64_t cluster_max_items(uint32_t tiles, uint32_t lodClusterMax);
 cudaError_t launch_cluster_cull(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s);
