@@ -13,9 +13,9 @@
 //            documented form (VendorCode/Meshoptimizer/meshoptimizer.h:561-569). A visible cluster
 //            sets its bit in the tile's slot-ordered visibility words and counts towards its tile
 //            and the frame;
-//   emit     one warp per tile with records: the records of the tiles before it (a strided sum of
-//            their counts), then a record for every set bit at its final position, without
-//            repeating a test.
+//   emit     one warp per tile with records: the records of the tiles before it (from the counts
+//            per group of 64 tiles, which the test launch also keeps), then a record for every set
+//            bit at its final position, without repeating a test.
 // Nothing is materialised per candidate cluster but its bit.
 //
 // The task form (mesh-shader consumers) runs the same tests; its test launch also counts each
@@ -231,8 +231,9 @@ __global__ void __launch_bounds__(kClThreads) cluster_test_kernel(const ClusterP
 // Emit launch, one warp per tile (lane = object): no test is repeated. The last tile's warp writes
 // the frame's counts; a tile without records returns. The tile's cluster ranges, visibility bits
 // and counts come from the earlier launches, the records (task form: tasks and payloads) before it
-// from the counts of the tiles before it; every set bit is written at its final position in slot
-// order, the tile's set bits spread over the lanes 32 at a time.
+// from the counts of the groups of tiles before its group and of the tiles of its group before it;
+// every set bit is written at its final position in slot order, the tile's set bits spread over
+// the lanes 32 at a time.
 template <bool TASKS>
 __global__ void __launch_bounds__(kClThreads) cluster_emit_kernel(const ClusterParams p) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
