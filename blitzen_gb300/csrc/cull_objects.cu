@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) cull_frame_kernel(con
 // rewinds the decide kernel's work counter for the next launch.
 constexpr int kScatterWarps = 32;  // one warp per chunk
 constexpr uint32_t kScatterChunks = 32;
-constexpr uint32_t kScatterPre = 2;  // 32-record slices of its chunk a warp loads before the offsets are known
+constexpr uint32_t kScatterPre = 3;  // 32-record slices of its chunk a warp loads before the offsets are known
 
 template <bool SINGLE>
 __device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_t block) {
@@ -553,24 +553,13 @@ __device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_
     if (c0 >= p.totalTiles) return;
     const uint32_t vi0 = SINGLE ? 0u : find_view_warp(p.tileStart, p.viewCount, c0);
     const uint32_t viewStart0 = SINGLE ? 0u : __ldg(p.tileStart + vi0);
-    // 0. each warp fetches its chunk's first kScatterPre * 32 staged records and their LODs now, so
-    //    those loads overlap the offset computation below
+    // 0. each warp fetches its chunk's count (handed to warp 0 through shared memory) and, once it
+    //    is known, its first kScatterPre * 32 staged records, which arrive while the block scans;
+    //    their LODs are fetched after the barrier
     const uint32_t myChunk = c0 + warp;
     const uint32_t myN = myChunk < p.totalTiles ? __ldcg(p.chunkCount + myChunk) : 0u;
     const uint2* myStage = p.staged + static_cast<size_t>(myChunk) * chunkSize;
-    uint2 pre[kScatterPre], preLod[kScatterPre];
-#pragma unroll
-    for (uint32_t u = 0; u < kScatterPre; ++u) {
-        const uint32_t i = lane + 32u * u;
-        pre[u] = i < myN ? __ldcg(myStage + i) : make_uint2(0u, 0u);
-    }
-#pragma unroll
-    for (uint32_t u = 0; u < kScatterPre; ++u) {
-        const uint32_t i = lane + 32u * u;
-        preLod[u] = i < myN ? __ldg(reinterpret_cast<const uint2*>(p.sc.lods + pre[u].y)) : make_uint2(0u, 0u);
-    }
-    // 1. records of the first chunk's view before c0; each warp also hands its chunk's count to
-    //    warp 0 through shared memory
+    // 1. records of the first chunk's view before c0, loaded while the count is on its way
     uint32_t part = 0;
     for (uint32_t c = viewStart0 + threadIdx.x; c < c0; c += 8u * kScatterWarps * 32u) {
         uint32_t x[8];  // eight loads in flight per thread
@@ -582,6 +571,12 @@ __device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_
 #pragma unroll
         for (uint32_t k = 0; k < 8u; ++k) part += x[k];
     }
+    uint2 pre[kScatterPre], preLod[kScatterPre];
+#pragma unroll
+    for (uint32_t u = 0; u < kScatterPre; ++u) {
+        const uint32_t i = lane + 32u * u;
+        pre[u] = i < myN ? __ldcg(myStage + i) : make_uint2(0u, 0u);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
     if (lane == 0) {
@@ -589,6 +584,11 @@ __device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_
         s_n[warp] = myN;
     }
     __syncthreads();
+#pragma unroll
+    for (uint32_t u = 0; u < kScatterPre; ++u) {
+        const uint32_t i = lane + 32u * u;
+        preLod[u] = i < myN ? __ldg(reinterpret_cast<const uint2*>(p.sc.lods + pre[u].y)) : make_uint2(0u, 0u);
+    }
     // 2. warp 0: exclusive offsets of the block's chunks, a scan restarting at each view's first chunk
     if (warp == 0) {
         uint32_t carry = 0;
@@ -664,14 +664,14 @@ __device__ __forceinline__ void scatter_block(const PipeParams& p, const uint32_
 }
 
 template <bool SINGLE>
-__global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter_kernel(const PipeParams p) {
+__global__ void __launch_bounds__(kScatterWarps * 32, 2) cull_scatter_kernel(const PipeParams p) {
     scatter_block<SINGLE>(p, blockIdx.x);
 }
 
 // Both record lists of a one-call frame in one launch: blocks [0, blocks1) scatter list 1, the rest
 // list 2. Block 0 also rewinds the frame kernel's pyramid ticket, tile count and ready flag (the
 // frame kernel has finished: this launch follows it on the stream).
-__global__ void __launch_bounds__(kScatterWarps * 32) cull_scatter2_kernel(const PipeParams p1, const PipeParams p2,
+__global__ void __launch_bounds__(kScatterWarps * 32, 2) cull_scatter2_kernel(const PipeParams p1, const PipeParams p2,
                                                                            const uint32_t blocks1) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         p1.scratch->frameTicket = 0u;
