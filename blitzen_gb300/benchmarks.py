@@ -39,7 +39,10 @@ def _camera_to_world(view: abi.CameraViewData, p: np.ndarray, position) -> np.nd
     return (p.astype(np.float64) @ rot.T + np.asarray(position, np.float64)).astype(np.float32)
 
 
-def build_views(culler, scene, device, n_views=64, seed=0, lo=1000, hi=2_000_000):
+def build_views(culler, scene, device, n_views=64, seed=0, lo=1000, hi=2_000_000, boxes_out=None):
+    """The batched-views workload: per view a camera, a render list (a subset of the scene), an
+    occluder depth rasterised on the GPU and its pyramid, and an output. `boxes_out`, when a list,
+    receives each view's occluder boxes (world space), so that a check can rebuild the depth."""
     specs = S.multiview_specs(scene.count, n_views, seed=seed, lo=lo, hi=hi)
     rng = np.random.default_rng(seed + 7)
     views = (BatchView * n_views)()
@@ -53,6 +56,8 @@ def build_views(culler, scene, device, n_views=64, seed=0, lo=1000, hi=2_000_000
         lo_w = _camera_to_world(v, boxes_cam[:, :3], sp.position)
         hi_w = _camera_to_world(v, boxes_cam[:, 3:], sp.position)
         boxes = np.concatenate([np.minimum(lo_w, hi_w), np.maximum(lo_w, hi_w)], axis=1).astype(np.float32)
+        if boxes_out is not None:
+            boxes_out.append(boxes)
         depth = torch.zeros(W * H, dtype=torch.float32, device=device)
         culler.raster_boxes(v, torch.from_numpy(boxes.reshape(-1)).to(device), depth, W, H)
         pyr = DevicePyramid(W, H, abi.HIZ_D3D12, device)

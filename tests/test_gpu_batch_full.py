@@ -1,7 +1,8 @@
 """The batched-views workload at full size (64 views over the 4M-object stress scene, log-uniform
 1k..2M objects per view, each with its own rasterised depth and pyramid, frustum + Hi-Z + LOD),
 batched in one launch under every supported launch shape and every chunk size, compared view by view
-with the oracle."""
+with the oracle. Each view's depth and pyramid are rebuilt by the oracle from the view's occluder
+boxes; the GPU's pyramids must equal them and the oracle culls against its own."""
 import numpy as np
 import pytest
 
@@ -27,14 +28,17 @@ def full(lib):
     c = Culler(0)
     sc = S.stress_scene(4_000_000, seed=0)
     c.setup_for_rendering(sc)
-    views, keep, _ = B.build_views(c, sc, c.device, n_views=64)
+    boxes = []
+    views, keep, _ = B.build_views(c, sc, c.device, n_views=64, boxes_out=boxes)
     specs = S.multiview_specs(sc.count, 64, seed=0, lo=1000, hi=2_000_000)
     threads = O.default_threads()
     ref = []
     for i, sp in enumerate(specs):
         objs, pyr, t = keep[i]
-        hp = O.HostPyramid(B.W, B.H, abi.HIZ_D3D12)
-        hp.data[:] = pyr.storage.cpu().numpy()
+        # the view's occluder depth and pyramid rebuilt by the oracle, and the GPU's pyramid (rastered
+        # and reduced on the GPU) checked against it texel for texel; the oracle culls against its own
+        hp = O.pyramid_build(O.depth_raster(views[i].view, boxes[i], B.W, B.H))
+        assert np.array_equal(pyr.storage.cpu().numpy().view(np.uint32), hp.data.view(np.uint32)), f"view {i}: pyramid"
         n, recs, _ = O.cull(abi.MODE_TEMPORAL, views[i].view, sc, objects=S.subset_objects(sc, sp.subset),
                             pyramid=hp, stride=t.stride, threads=threads)
         ref.append((n, recs))
