@@ -165,6 +165,7 @@ int bind_cluster_scratch(blz_ctx* c, uint32_t tiles, ClusterParams& p) {
     p.objSurv = reinterpret_cast<uint32_t*>(m);
     m += survBytes;
     p.items = reinterpret_cast<uint4*>(m);
+    p.itemCapacity = static_cast<uint32_t>(std::min<uint64_t>(cluster_max_items(tiles, bitWords), 0xFFFFFFFFu));
     m += itemBytes;
     p.bits = reinterpret_cast<uint32_t*>(m);
     p.bitWords = bitWords;

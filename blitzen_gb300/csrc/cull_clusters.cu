@@ -151,8 +151,15 @@ __global__ void __launch_bounds__(kClThreads) cluster_object_kernel(const Cluste
     if (lane == 31 && itemTotal != 0u) itemBase = atomicAdd(p.itemCount, itemTotal);
     itemBase = __shfl_sync(0xFFFFFFFFu, itemBase, 31) + itemIncl - nItems;
     const uint32_t start = incl - count;  // the object's first slot
-    for (uint32_t q = 0; q < nItems; ++q)
-        p.items[itemBase + q] = make_uint4(i, clusterOffset + q * kClItem, start + q * kClItem, min(kClItem, count - q * kClItem));
+    // the list holds every item a call can make; a count left over by a call whose later launches
+    // never ran could still push past it, so nothing is written past the end (the test launch reads
+    // at most itemCapacity items, and the call is flagged)
+    for (uint32_t q = 0; q < nItems; ++q) {
+        if (itemBase + q < p.itemCapacity)
+            p.items[itemBase + q] = make_uint4(i, clusterOffset + q * kClItem, start + q * kClItem, min(kClItem, count - q * kClItem));
+        else
+            flags |= BLZ_FLAG_BAD_INDEX;
+    }
     uint32_t* bits = p.bits + static_cast<size_t>(tile) * p.bitWords;
     for (uint32_t w = lane; w < (total + 31u) / 32u; w += 32u) bits[w] = 0u;
     p.objInfo[i] = make_uint2(clusterOffset, count);
@@ -189,7 +196,7 @@ __device__ __forceinline__ void or_bits(uint32_t* bits, uint32_t s0, uint32_t ba
 template <bool TASKS>
 __global__ void __launch_bounds__(kClThreads) cluster_test_kernel(const ClusterParams p, const BlzCameraViewData view) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t nItems = __ldcg(p.itemCount);
+    const uint32_t nItems = min(__ldcg(p.itemCount), p.itemCapacity);
     const ViewConsts v = load_view(view);
     const uint32_t warpsTotal = gridDim.x * kClWarps;
     for (uint32_t it = blockIdx.x * kClWarps + warp; it < nItems; it += warpsTotal) {

@@ -171,6 +171,7 @@ struct ClusterParams {
     uint32_t* tileCount;  // scratch [tiles] uint2: {surviving clusters, 0} per tile (task form: {tasks, payloads})
     uint4* items;         // scratch: the test launch's work list, {object, first cluster, first slot, clusters}
     uint32_t* itemCount;  // scratch, one word: items in the list (zero between launches)
+    uint32_t itemCapacity; // items the list holds: every item the call's tiles can make
     uint2* totals;        // scratch: the frame's records (task form: {tasks, payloads}), counted by the test launch
     uint2* superCount;    // scratch [cluster_tile_groups(tiles)]: the same counts per group of tiles
     // task form (blz_cull_cluster_tasks)
