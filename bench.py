@@ -244,7 +244,7 @@ def recorded_traffic(kernels, objects: int):
         if any(int(e["objects"]) != objects for e in es):
             return None
         return {"bytes_per_launch": sum(int(e["dram_bytes_per_launch"]) for e in es),
-                "source": f"ncu capture at commit {d['commit']}: {d['command']}"}
+                "source": "; ".join(f"{k}: ncu capture at commit {e['commit']}: {e['command']}" for k, e in zip(kernels, es))}
     except Exception:
         return None
 
@@ -446,6 +446,10 @@ def main():
     if traffic:
         roofline["traffic"] = traffic["bytes_per_launch"]
         roofline["traffic_source"] = traffic["source"]
+    frame_traffic = recorded_traffic(("cull_frame_kernel<0,256,2>", "cull_scatter2_kernel"), args.objects)
+    if frame_traffic:
+        roofline["others"]["frame"]["traffic"] = frame_traffic["bytes_per_launch"]
+        roofline["others"]["frame"]["traffic_source"] = frame_traffic["source"]
 
     # ---------------- e2e through the C ABI with host buffers
     hdepth = torch.empty(W * H, dtype=torch.float32, pin_memory=True)
