@@ -982,7 +982,7 @@ cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t thre
 //   place    each warp places its records in order (ranks inside 32-record slices from one
 //            ballot per bit of the LOD id).
 
-constexpr uint32_t kInstBatch = 4;  // 32-record slices whose loads are issued together
+constexpr uint32_t kInstBatch = 5;  // 32-record slices whose loads are issued together (the first batch's ranks are kept)
 constexpr uint32_t kInstThreads = kInstGroup * 32;
 
 
@@ -1011,7 +1011,7 @@ __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStag
             r[k] = j < n ? __ldcg(st + j) : make_uint2(0u, 0xFFFFFFFFu);
         }
     };
-    uint2 first[kInstBatch];  // the chunk's first 128 records, loaded once for both walks
+    uint2 first[kInstBatch];  // the chunk's first kInstBatch * 32 records, loaded once for both walks
     load_batch(0, first);
     // LOD threadIdx.x's instanceOffset (nL <= kInstThreads), stored to shared memory once phase 1
     // is done, so no barrier waits for the load
@@ -1042,7 +1042,10 @@ __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStag
     }
     uint32_t* row = s_rows + warp * nL;
     const uint32_t lt = lanemask_lt();
-    // 1. this chunk's records per LOD (only this warp touches its row)
+    // 1. this chunk's records per LOD (only this warp touches its row); each of the first batch's
+    //    records also keeps its rank among the chunk's records of its LOD (the count before its
+    //    32-record slice, from the slice's lowest lane of that LOD, plus the lanes below it)
+    uint32_t rank[kInstBatch];
     for (uint32_t j0 = 0; j0 < n; j0 += 32u * kInstBatch) {
         uint2 r[kInstBatch];
         if (j0 == 0) {
@@ -1055,7 +1058,15 @@ __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStag
         for (uint32_t k = 0; k < kInstBatch; ++k) {
             const uint32_t b = r[k].y;
             const unsigned peers = same_lod_lanes(b, idBits, b != 0xFFFFFFFFu);
-            if (b != 0xFFFFFFFFu && (peers & lt) == 0u) row[b] += __popc(peers);
+            uint32_t before = 0;
+            if (b != 0xFFFFFFFFu && (peers & lt) == 0u) {
+                before = row[b];
+                row[b] = before + __popc(peers);
+            }
+            if (j0 == 0) {  // warp-uniform
+                before = __shfl_sync(0xFFFFFFFFu, before, (__ffs(peers) - 1) & 31);
+                rank[k] = before + __popc(peers & lt);
+            }
             __syncwarp();
         }
     }
@@ -1082,10 +1093,23 @@ __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStag
         }
     }
     __syncthreads();
-    // 3. place the records in object order
+    // 3. place the records in object order: a chunk the first batch holds whole places each record
+    //    at its LOD's group offset + the warp's offset + its rank; a longer one ranks its records
+    //    again, slice by slice
     const uint32_t slots = q.slotsPerLod ? q.slotsPerLod : 0xFFFFFFFFu;
     unsigned int flags = 0u;
-    for (uint32_t j0 = 0; j0 < n; j0 += 32u * kInstBatch) {
+    if (n <= 32u * kInstBatch) {
+#pragma unroll
+        for (uint32_t k = 0; k < kInstBatch; ++k) {
+            const uint32_t b = first[k].y;
+            if (b == 0xFFFFFFFFu) continue;
+            const uint32_t pos = s_goff[b] + row[b] + rank[k];
+            const uint64_t at = static_cast<uint64_t>(s_ioff[b]) + pos;
+            if (pos < slots && at < q.instanceCapacity) q.instances[at] = first[k].x;
+            else flags |= BLZ_FLAG_INSTANCE_OVERFLOW;
+        }
+    }
+    for (uint32_t j0 = 0; n > 32u * kInstBatch && j0 < n; j0 += 32u * kInstBatch) {
         uint2 r[kInstBatch];
         if (j0 == 0) {
 #pragma unroll

@@ -46,6 +46,34 @@ def test_instanced_matches_oracle(stress_ctx, slots):
     assert np.array_equal(dinst.cpu().numpy().view(np.uint32), oinst)
 
 
+def test_instanced_long_chunks_matches_oracle(lib):
+    """1M objects, every one in view: single-view chunks of 256 objects emit more records than the
+    place kernel's first batch holds (160), so this takes the path that ranks a chunk's records slice
+    by slice, beside the one that keeps the first batch's ranks."""
+    sc = S.stress_scene(1_000_000, seed=1)
+    c = Culler(0)
+    try:
+        c.setup_for_rendering(sc)
+        v = view_for(zfar=1e30, position=(0.0, 0.0, -20000.0))
+        slots = 100_000
+        ctr = O.new_counters(sc, slots)
+        cap = len(sc.lods) * slots
+        dctr = torch.from_numpy(ctr.view(np.int32).reshape(-1).copy()).cuda()
+        dinst = torch.full((cap,), -1, dtype=torch.int32, device="cuda")
+        t = Target.alloc(len(sc.lods), abi.STRIDE_D3D12)
+        c.draw_instance_cull_pass(v, dctr, dinst, slots, t)
+        flags = c.flags()
+        n, cmds, octr, oinst, oflags = O.cull_instanced(v, sc, ctr, cap, slots, stride=abi.STRIDE_D3D12)
+        visible = int(octr.view(np.uint32).reshape(-1, 2)[:, 1].sum())
+        assert visible > 0.9 * sc.count, visible
+        assert flags == oflags == 0
+        assert_records_equal(t.read(), (n, cmds), "instanced commands")
+        assert np.array_equal(dctr.cpu().numpy().view(np.uint32), octr.view(np.uint32).reshape(-1))
+        assert np.array_equal(dinst.cpu().numpy().view(np.uint32), oinst)
+    finally:
+        c.close()
+
+
 def test_instanced_empty_view(stress_ctx):
     c, sc = stress_ctx
     v = view_for(zfar=1e4, position=(0.0, 0.0, 1e7))  # every object behind the camera
