@@ -975,9 +975,9 @@ cudaError_t launch_object_cull(uint32_t mode, const PipeParams& p, uint32_t thre
 // also counts each group's records per LOD (hist[group][lod], groups of kInstGroup chunks, zeroed
 // before the launch), and then one place launch, a block per group:
 //   offsets  each LOD's offset for the group is the sum of the LOD's counts in the groups before it
-//            (coalesced loads across LODs, the block's threads taking interleaved groups); block 0,
-//            which has no group before it, sums all of them instead, which gives every LOD's total,
-//            and writes the counters and, in ascending LOD order, one command per non-empty LOD;
+//            (coalesced loads across LODs, the block's threads taking interleaved groups); the last
+//            group's block adds its own group's counts, which gives every LOD's total, and writes
+//            the counters and, in ascending LOD order, one command per non-empty LOD;
 //   rows     each warp counts its chunk's records per LOD, and the block scans those rows per LOD;
 //   place    each warp places its records in order (ranks inside 32-record slices from one
 //            ballot per bit of the LOD id).
@@ -988,7 +988,7 @@ constexpr uint32_t kInstThreads = kInstGroup * 32;
 
 __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStagedParams q) {
     // [kInstGroup][nL] per-warp counts, then offsets; [nL] the group's offset in each LOD's list;
-    // [nL] each LOD's instanceOffset; [nL] (block 0) each LOD's total; [R][nL] partial sums
+    // [nL] each LOD's instanceOffset; [nL] (the last group's block) each LOD's total; [R][nL] partial sums
     extern __shared__ uint32_t s_rows[];
     __shared__ unsigned int s_flags;
     __shared__ uint32_t s_warpSums[32];
@@ -1025,10 +1025,9 @@ __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStag
     if (threadIdx.x == 0) s_flags = 0u;
     __syncthreads();
     // 0. the group's offset in each LOD's list: the LOD's counts of the groups before this one,
-    //    row tr taking every R-th group (coalesced across LODs). Block 0, which has none before
-    //    it, sums every group instead: each LOD's total, for the commands (step 4).
+    //    row tr taking every R-th group (coalesced across LODs)
     if (tr < R) {
-        const uint32_t g1 = g == 0 ? G : g;
+        const uint32_t g1 = g;
         uint32_t sum = 0, gg = tr;
         for (; gg + 7u * R < g1; gg += 8u * R) {  // eight loads in flight at a time
             uint32_t x[8];
@@ -1038,7 +1037,7 @@ __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStag
             for (uint32_t k = 0; k < 8u; ++k) sum += x[k];
         }
         for (; gg < g1; gg += R) sum += __ldcg(q.hist + static_cast<size_t>(gg) * nL + tb);
-        if (sum) atomicAdd(g == 0 ? &s_tot[tb] : &s_goff[tb], sum);
+        if (sum) atomicAdd(&s_goff[tb], sum);
     }
     uint32_t* row = s_rows + warp * nL;
     const uint32_t lt = lanemask_lt();
@@ -1134,9 +1133,13 @@ __global__ void __launch_bounds__(kInstThreads) inst_place_kernel(const InstStag
             __syncwarp();
         }
     }
-    // 4. block 0: the counters and, in ascending LOD order, one command per non-empty LOD
+    // 4. the last group's block: every LOD's total is its group offset plus its own group's count;
+    //    then the counters and, in ascending LOD order, one command per non-empty LOD
     //    (drawInstCmd.cs.hlsl:9-38)
-    if (g == 0) {
+    if (g == G - 1u) {
+        for (uint32_t l = threadIdx.x; l < nL; l += kInstThreads)
+            s_tot[l] = s_goff[l] + __ldcg(q.hist + static_cast<size_t>(g) * nL + l);
+        __syncthreads();
         const uint32_t perT = (nL + kInstThreads - 1u) / kInstThreads;
         const uint32_t b0 = min(nL, threadIdx.x * perT), b1 = min(nL, b0 + perT);
         uint32_t mine = 0;
