@@ -174,6 +174,22 @@ int bind_cluster_scratch(blz_ctx* c, uint32_t tiles, ClusterParams& p) {
     return BLZ_OK;
 }
 
+// The cluster test kernel's resident blocks per SM for the records (tasks false) or task form, found
+// on the context's first call of that form (which allocates the cluster scratch, so it never runs
+// inside a capture) and kept in the context.
+int cluster_test_occupancy(blz_ctx* c, bool tasks, ClusterParams& p) {
+    int& n = c->clusterTestBlocksPerSm[tasks ? 1 : 0];
+    if (n == 0) {
+        const cudaError_t e = cluster_test_blocks_per_sm(tasks, &n);
+        if (e != cudaSuccess) {
+            n = 0;
+            return cuda_fail(e, "cluster test kernel occupancy");
+        }
+    }
+    p.testBlocksPerSm = static_cast<uint32_t>(n);
+    return BLZ_OK;
+}
+
 void bind_chunk_scratch(blz_ctx* c, PipeParams& p) {
     char* m = static_cast<char*>(c->chunkMem);
     p.staged = reinterpret_cast<uint2*>(m);
@@ -1001,6 +1017,8 @@ int blz_cull_clusters(blz_ctx* c, const BlzCameraViewData* view, BlzRenderList l
     ClusterParams p{};
     rc = bind_cluster_scratch(c, tiles, p);
     if (rc != BLZ_OK) return rc;
+    rc = cluster_test_occupancy(c, false, p);
+    if (rc != BLZ_OK) return rc;
     p.sc = c->scene;
     p.objects = objs;
     p.count = count;
@@ -1039,6 +1057,8 @@ int blz_cull_cluster_tasks(blz_ctx* c, const BlzCameraViewData* view, BlzRenderL
     if (tiles == 0) tiles = 1;
     ClusterParams p{};
     rc = bind_cluster_scratch(c, tiles, p);
+    if (rc != BLZ_OK) return rc;
+    rc = cluster_test_occupancy(c, true, p);
     if (rc != BLZ_OK) return rc;
     p.sc = c->scene;
     p.objects = objs;

@@ -47,6 +47,7 @@ struct blz_ctx {
     size_t instWords = 0;
     void* clusterMem = nullptr;        // cluster cull: tile counts, object ranges and survivors, visibility bits
     size_t clusterBytes = 0;
+    int clusterTestBlocksPerSm[2] = {0, 0};  // records, task form: resident test blocks per SM (found on first use)
     uint32_t lodClusterMax = 0;        // largest clusterCount of the scene's LODs (clamped to the cluster table)
     bool hasScene = false;
     blz::SceneT scene{};

@@ -404,20 +404,22 @@ static cudaError_t launch_cluster(const ClusterParams& p, const BlzCameraViewDat
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     // the test launch: every resident warp at once, or one warp per item when there are fewer
-    static int perSm = 0;
-    if (perSm == 0) {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, cluster_test_kernel<TASKS>, kClThreads, 0);
-        if (e != cudaSuccess) return e;
-        if (perSm < 1) perSm = 1;
-    }
     const uint64_t maxItems = cluster_max_items(p.tiles, p.bitWords);
-    uint64_t blocks = static_cast<uint64_t>(perSm) * (p.smCount > 0 ? p.smCount : 1);
+    uint64_t blocks = static_cast<uint64_t>(p.testBlocksPerSm > 0 ? p.testBlocksPerSm : 1) * (p.smCount > 0 ? p.smCount : 1);
     blocks = std::min<uint64_t>(blocks, (maxItems + kClWarps - 1) / kClWarps);
     cluster_test_kernel<TASKS><<<static_cast<uint32_t>(blocks ? blocks : 1), kClThreads, 0, s>>>(p, view);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     cluster_emit_kernel<TASKS><<<(p.tiles + kClWarps - 1) / kClWarps, kClThreads, 0, s>>>(p);
     return cudaGetLastError();
+}
+
+cudaError_t cluster_test_blocks_per_sm(bool tasks, int* out) {
+    *out = 0;
+    cudaError_t e = tasks ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, cluster_test_kernel<true>, kClThreads, 0)
+                          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, cluster_test_kernel<false>, kClThreads, 0);
+    if (e == cudaSuccess && *out < 1) *out = 1;
+    return e;
 }
 
 uint64_t cluster_max_items(uint32_t tiles, uint32_t lodClusterMax) {

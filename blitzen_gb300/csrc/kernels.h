@@ -188,6 +188,7 @@ struct ClusterParams {
     uint32_t bitWords;       // words per tile: >= 32 objects x the largest LOD cluster count / 32
     uint32_t tiles;          // tiles of 32 objects
     uint32_t smCount;        // the device's SMs (the test launch is one wave of resident blocks)
+    uint32_t testBlocksPerSm; // resident blocks of the test kernel per SM
     uint32_t* tileSlots;     // scratch [tiles]: candidate clusters of the tile
 };
 
@@ -254,6 +255,8 @@ cudaError_t launch_instanced_cull(const InstancedParams& p, const BlzCameraViewD
 uint32_t cluster_tile_objects();
 // Groups of tiles whose counts the cluster test launch also sums, for `tiles` tiles.
 uint32_t cluster_tile_groups(uint32_t tiles);
+// Resident blocks per SM of the cluster test kernel (records or task form) on the current device.
+cudaError_t cluster_test_blocks_per_sm(bool tasks, int* out);
 // Upper bound of the cluster test launch's work items for `tiles` tiles.
 uint64_t cluster_max_items(uint32_t tiles, uint32_t lodClusterMax);
 cudaError_t launch_cluster_cull(const ClusterParams& p, const BlzCameraViewData& view, cudaStream_t s);
